@@ -1,0 +1,395 @@
+"""Benchmark of the voxel ray tracer on GB300: Mrays/s of the 1080p / 16-light frame.
+
+One step = one frame of the full scene: world 512x256x512 (seeded terrain, resident in
+HBM), 1920x1080, 16 local lights + the global light, 1024 DDA steps per ray; rays =
+primary rays + shadow rays actually cast (counted on the device, equal to the oracle's
+count).  L2 is flushed (a 256 MiB write) before every timed frame; each frame is timed
+with CUDA events on the launching stream.
+
+  value      Mrays/s of vrt_render (device buffers), whole job over N GPUs (replicas)
+  e2e        the same through vrt_render_to_host: uniforms in, RGBA8 image copied to
+             pinned host memory every step, wall clock
+  roofline   effective bytes B = 4*steps + 4*primary hits + 4*pixels per frame (one
+             4-byte voxel word per DDA step in the reference shader) / kernel time,
+             against the measured HBM copy bandwidth; l2 fields against a measured L2
+             read bandwidth
+  batched    64 cameras of uneven size in one CUDA-graph-captured persistent launch vs
+             one launch per camera
+  served     Poisson stream over 4 resident worlds: p50/p99 latency and Mrays/s per rate
+  cpu_baseline  the CPU oracle (scalar C++ restatement of the shader, OpenMP over rows)
+             on a bounded row sample of the same frame
+
+--impl reference times the CPU restatement of the reference shader (the reference
+itself is a GLSL fragment shader; it cannot run here) on all host cores.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "voxel-rt_gb300"))
+
+METRIC = "Mrays/s @1080p 16 lights; served p50/p99 ms vs plain per-frame launch"
+UNIT = "Mrays/s"
+
+
+def rank_info():
+    return int(os.environ.get("RANK", "0")), int(os.environ.get("WORLD_SIZE", "1")), int(os.environ.get("LOCAL_RANK", "0"))
+
+
+def measured_peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as f:
+            d = json.load(f)
+        return float(d.get("hbm_gbs", 6800.0)), "measured"
+    return 6800.0, "fallback"
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons, sampled every 200 ms while running."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.gpu), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if not self.proc:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except Exception:
+            self.proc.kill()
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            parts = [p.strip() for p in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, parts[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        import statistics
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+def cpu_baseline(scene, target_s: float, threads: int):
+    """Oracle (-O3, no contraction, OpenMP over rows) on the same frame: whole frames
+    repeated until about target_s of CPU time, or an even row sample when one frame
+    alone would take longer."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import vrt_oracle
+    vrt_oracle.build()
+    u = scene.uniforms
+    t0 = time.perf_counter()
+    probe = vrt_oracle.render(scene.words, scene.W, scene.H, u, scene.width, scene.height,
+                              rows=(0, scene.height, 30), threads=threads, fast=True, outputs=False)
+    est_frame = max(time.perf_counter() - t0, 1e-4) * 30.0
+    stride = 1 if est_frame <= target_s else max(1, int(round(est_frame / target_s)))
+    reps = max(1, min(50, int(target_s / est_frame))) if stride == 1 else 1
+    rays, dt = 0, 0.0
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        res = vrt_oracle.render(scene.words, scene.W, scene.H, u, scene.width, scene.height,
+                                rows=(0, scene.height, stride), threads=threads, fast=True, outputs=False)
+        dt += time.perf_counter() - t0
+        rays += res["totals"]["rays"]
+    nrows = len(range(0, scene.height, stride))
+    what = (f"{reps} whole {scene.width}x{scene.height} frames" if stride == 1 else
+            f"every {stride}th row of the {scene.width}x{scene.height} frame ({nrows} rows)")
+    return {"value": rays / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+            "sample": f"{what}: {rays} rays in {dt:.2f} s", "seconds": dt / reps}
+
+
+def run_reference(args):
+    rank, world_size, _ = rank_info()
+    if rank != 0:
+        return 0
+    import scenes
+    threads = os.cpu_count() or 1
+    sc = scenes.full(2, threads=threads)
+    steps = []
+    for i in range(args.warmup + args.steps):
+        r = cpu_baseline(sc, args.cpu_seconds / 2.0, threads)
+        if i >= args.warmup:
+            steps.append(r)
+    val = sum(s["value"] for s in steps) / len(steps)
+    ms = sum(s["seconds"] for s in steps) / len(steps) * 1000.0
+    line = {
+        "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world_size,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded terrain)",
+        "config": {"workload": sc.workload, "sample": steps[-1]["sample"]},
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": steps[-1]["sample"]},
+        "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "the reference path is a GLSL fragment shader (no graphics stack here); its CPU restatement "
+                "(the oracle, bit-exact with the shader source compiled via GLM) is timed on all host cores",
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def load_traffic(kernel: str, workload: str):
+    p = os.path.join(ROOT, "profiles", "traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    e = d.get(kernel, {})
+    return e.get("bytes_per_launch") if e.get("workload") == workload else None
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-extras", action="store_true", help="skip the batched / served / CPU legs")
+    ap.add_argument("--kernel", default="mask", choices=["mask", "word"])
+    ap.add_argument("--tile", default="8x4")
+    ap.add_argument("--refill", type=int, default=8)
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+
+    import numpy as np
+    import torch
+
+    import build as vbuild
+    import scenes
+    import vrt
+
+    rank, world_size, local_rank = rank_info()
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world_size > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    if rank == 0 or world_size == 1:
+        vbuild.build()
+    if dist:
+        dist.barrier()
+    vrt.lib()
+    dev = torch.device("cuda", local_rank)
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    threads = max(1, (os.cpu_count() or 1) // max(1, world_size))
+    sc = scenes.full(2, threads=threads)
+    world = vrt.World(sc.W, sc.H)
+    world.upload(sc.words)
+    r = vrt.Renderer()
+    opts = vrt.RenderOpts()
+    opts.kernel = vrt.KERNEL_BITMASK if args.kernel == "mask" else vrt.KERNEL_WORD
+    opts.tile_w, opts.tile_h = (int(v) for v in args.tile.split("x"))
+    opts.refill_min = args.refill
+    W, H = sc.width, sc.height
+    img = torch.empty(W * H * 4, dtype=torch.uint8, device=dev)
+    stats = torch.zeros(vrt.STAT_COUNT, dtype=torch.int64, device=dev)
+    r.render(world, sc.uniforms, W, H, img.data_ptr(), None, stats.data_ptr(), opts, sh)
+    torch.cuda.synchronize()
+    st = stats.cpu().numpy()
+    rays, steps, hits, pixels = (int(st[i]) for i in range(4))
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+
+    for _ in range(args.warmup):
+        r.render(world, sc.uniforms, W, H, img.data_ptr(), None, 0, opts, sh)
+    torch.cuda.synchronize()
+    clocks = ClockSampler(local_rank)
+    clocks.start()
+    time.sleep(0.3)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+    for a, b in evs:
+        flush.zero_()  # evict L2 (256 MiB > 129 MB) outside the timed span
+        a.record(stream)
+        r.render(world, sc.uniforms, W, H, img.data_ptr(), None, 0, opts, sh)
+        b.record(stream)
+    torch.cuda.synchronize()
+    if dist:
+        dist.barrier()
+    clk = clocks.stop()
+    times = [a.elapsed_time(b) for a, b in evs]
+    ms = sum(times) / len(times)
+    if dist:
+        t = torch.tensor([ms], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        ms = float(t.item())
+    value = world_size * rays / (ms * 1e-3) / 1e6
+
+    # end to end through the public API: uniforms in, image out to pinned host memory
+    host = torch.empty(W * H * 4, dtype=torch.uint8, pin_memory=True)
+    for _ in range(2):
+        r.render_to_host(world, sc.uniforms, W, H, host.data_ptr(), opts, sh)
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        r.render_to_host(world, sc.uniforms, W, H, host.data_ptr(), opts, sh)
+    e2e_s = (time.perf_counter() - t0) / args.steps
+    if dist:
+        t = torch.tensor([e2e_s], device=dev)
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    e2e = {"value": world_size * rays / e2e_s / 1e6, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
+           "h2d_bytes_per_step": int(C_sizeof_uniforms()), "d2h_bytes_per_step": W * H * 4}
+
+    peak, peak_src = measured_peaks()
+    algo_bytes = 4 * steps + 4 * hits + 4 * pixels
+    achieved = algo_bytes / (ms * 1e-3) / 1e9
+    kname = "render_mask_kernel" if args.kernel == "mask" else "render_word_kernel"
+    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
+                "traffic": load_traffic(kname, "full"), "peak_source": peak_src,
+                "algorithmic_bytes_per_launch": algo_bytes, "kernel": kname,
+                "note": "effective bytes: one 4-byte word per DDA step as the shader reads; the mask kernel reads "
+                        "far fewer physical bytes (traffic)"}
+
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded terrain, seed 2)",
+        "config": {"workload": sc.workload, "rays_per_frame": rays, "dda_steps_per_frame": steps,
+                   "primary_hits": hits, "pixels": pixels, "kernel": kname, "tile": args.tile,
+                   "refill_min": args.refill, "l2": "flushed before every timed frame (256 MiB write)",
+                   "parallelism": f"replicas x{world_size}"},
+        "clocks": clk, "gpu_launches": args.steps, "roofline": roofline, "e2e": e2e,
+        "frame_ms_min": min(times), "frame_ms_max": max(times),
+    }
+    if rank == 0:
+        try:
+            l2 = vrt.probe_l2_read_gbs(64 << 20, 100)
+            roofline["l2_read_gbs_measured"] = l2
+            roofline["l2_frac"] = achieved / l2
+        except Exception as e:  # measurement helper only
+            roofline["l2_read_gbs_measured"] = f"failed: {e}"
+    if rank == 0 and world_size == 1 and not args.no_extras:
+        line["batched"] = bench_batched(vrt, torch, scenes, sc, world, r, dev, stream)
+        line["served"] = bench_served(vrt, torch, scenes, sc, world)
+        line["served"]["plain_frame_ms"] = ms
+        line["cpu_baseline"] = cpu_baseline(sc, args.cpu_seconds, os.cpu_count() or 1)
+    if rank == 0:
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+    return 0
+
+
+def C_sizeof_uniforms():
+    import ctypes
+    import vrt
+    return ctypes.sizeof(vrt.Uniforms)
+
+
+def bench_batched(vrt, torch, scenes, sc, world, r, dev, stream):
+    """64 cameras in one graph-captured persistent launch vs one launch per camera."""
+    import ctypes as C
+    views = scenes.batch_views(sc, 64, seed=3)
+    imgs = [torch.empty(w * h * 4, dtype=torch.uint8, device=dev) for (_, w, h) in views]
+    stats = torch.zeros((len(views), vrt.STAT_COUNT), dtype=torch.int64, device=dev)
+    vv = [vrt.make_view(world, u, w, h, im.data_ptr(), stats[i].data_ptr())
+          for i, ((u, w, h), im) in enumerate(zip(views, imgs))]
+    sh = stream.cuda_stream
+    r.render_batch(vv, None, sh)
+    torch.cuda.synchronize()
+    rays = int(stats[:, vrt.STAT_RAYS].sum().item())
+    arr = (vrt.View * len(vv))(*vv)
+    vv_nostats = [vrt.make_view(world, u, w, h, im.data_ptr(), 0) for ((u, w, h), im) in zip(views, imgs)]
+    arr2 = (vrt.View * len(vv_nostats))(*vv_nostats)
+    g = C.c_void_p()
+    vrt.check(vrt.lib().vrt_batch_graph_create(r.handle, arr2, len(vv_nostats), None, sh, C.byref(g)))
+    for _ in range(2):
+        vrt.check(vrt.lib().vrt_batch_graph_launch(g, sh))
+    torch.cuda.synchronize()
+    a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    reps = 3
+    a.record(stream)
+    for _ in range(reps):
+        vrt.check(vrt.lib().vrt_batch_graph_launch(g, sh))
+    b.record(stream)
+    torch.cuda.synchronize()
+    batched_ms = a.elapsed_time(b) / reps
+    vrt.lib().vrt_batch_graph_destroy(g)
+    # plain: one vrt_render launch per camera
+    for (u, w, h), im in zip(views, imgs):
+        r.render(world, u, w, h, im.data_ptr(), None, 0, None, sh)
+    torch.cuda.synchronize()
+    a.record(stream)
+    for _ in range(reps):
+        for (u, w, h), im in zip(views, imgs):
+            r.render(world, u, w, h, im.data_ptr(), None, 0, None, sh)
+    b.record(stream)
+    torch.cuda.synchronize()
+    plain_ms = a.elapsed_time(b) / reps
+    return {"cameras": len(views), "pixels": sum(w * h for _, w, h in views), "rays": rays,
+            "batched_ms": batched_ms, "batched_mrays_per_s": rays / (batched_ms * 1e-3) / 1e6,
+            "plain_ms": plain_ms, "plain_mrays_per_s": rays / (plain_ms * 1e-3) / 1e6,
+            "speedup": plain_ms / batched_ms}
+
+
+def bench_served(vrt, torch, scenes, sc, full_world):
+    """4 resident worlds (256^3, 512x256x512, 1024x256x1024 x2), Poisson arrivals."""
+    import serving
+    threads = os.cpu_count() or 1
+    specs = []
+    worlds = [scenes.full(21, W=256, H=256, threads=threads), sc,
+              scenes.full(22, W=1024, H=256, threads=threads), scenes.full(23, W=1024, H=256, threads=threads)]
+    for i, s in enumerate(worlds):
+        w = full_world if s is sc else vrt.World(s.W, s.H)
+        if s is not sc:
+            w.upload(s.words)
+            s.words = None
+        specs.append(serving.WorldSpec(s, w))
+    srv = serving.Server(40 << 30, slots=4, max_batch=8)
+    wids = [srv.add_world(s.world) for s in specs]
+    results = []
+    for rate in (50.0, 200.0, 800.0):
+        reqs = serving.make_requests(specs, rate, 1.5, seed=int(rate))
+        done, wall = serving.run_open_loop(srv, wids, reqs)
+        res = serving.summarize(done, wall)
+        res["rate_hz"] = rate
+        results.append(res)
+    srv.close()
+    full_world.upload(sc.words)  # the served edits changed the shared world: restore it
+    return {"worlds": ["256x256x256", "512x256x512", "1024x256x1024", "1024x256x1024"], "budget_gib": 40,
+            "slots": 4, "max_batch": 8, "sweep": results}
+
+
+if __name__ == "__main__":
+    sys.exit(main())

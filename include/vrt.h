@@ -1,0 +1,279 @@
+/*
+ * vrt.h -- C ABI of the GB300 voxel ray tracer.
+ *
+ * This is the drop-in boundary for the per-pixel ray tracer of Berry2460/voxel-rt
+ * (src/fshader.glsl).  In the reference, the host talks to the GPU through OpenGL:
+ *   - the world is an SSBO of int32 voxel words (render.cpp:366-369, :199-223),
+ *   - the camera/light state is a set of glUniform* calls (render.cpp:289-296),
+ *   - a frame is glDrawArrays(GL_TRIANGLES, 0, 6) over a fullscreen quad (main.cpp:59).
+ * Here the world is a device-resident buffer owned by a vrt_world, the uniforms are a
+ * plain struct passed by pointer, and a frame is one kernel launch into a caller-owned
+ * device RGBA8 buffer.  Block destruction (level.cpp:30-56) and the depth field
+ * (render.cpp:226-253) become device-side scatter kernels.
+ *
+ * Conventions
+ *   - Every entry point returns an int status: 0 = ok, negative = error (VRT_E*).
+ *     vrt_last_error() returns a message for the calling thread's last failure.
+ *   - Streams are passed as void* (a cudaStream_t; NULL = legacy default stream).
+ *     All work is stream ordered; no call synchronises unless documented.
+ *   - Output buffers are caller-owned device memory unless the name says _host.
+ *   - Distinct worlds/renderers may be used from distinct threads; one object is
+ *     externally synchronised.
+ *
+ * Voxel word (fshader.glsl:12-15, README.md:5, render.cpp:189-196)
+ *   int32 per voxel at index x + W*y + W*H*z, with x,z in [0,W) and y in [0,H).
+ *   v >= 0       solid; colour R = (v>>16)&255, G = (v>>8)&255, B = v&255.
+ *   v == -1      empty air.
+ *   other v < 0  air carrying a depth-field skip distance: the float whose bits
+ *                are v is negative and the ray jumps -asfloat(v) voxels
+ *                (fshader.glsl:114-121, written by render.cpp:249-251).
+ *   Bit 24 is a free "solid" tag for generated worlds (0x01000000|rgb); it is
+ *   never tested: only the sign decides.
+ */
+#ifndef VRT_H
+#define VRT_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VRT_MAX_LOCAL_LIGHTS 16 /* MAX_LOCAL_LIGHTS, render.hpp:11 / fshader.glsl:6 */
+
+/* status codes */
+#define VRT_OK 0
+#define VRT_EINVAL -1     /* bad argument */
+#define VRT_ECUDA -2      /* a CUDA runtime call failed */
+#define VRT_ENOMEM -3     /* device or host allocation failed */
+#define VRT_ERANGE -4     /* size beyond a documented maximum */
+#define VRT_ETIMEOUT -5   /* a bounded device-side wait gave up */
+#define VRT_EBUDGET -6    /* request refused by the memory budget */
+#define VRT_ENOTFOUND -7  /* unknown id */
+#define VRT_ESTATE -8     /* object in the wrong state for this call */
+
+/* Uniform block of fshader.glsl:20-26 plus the constants of fshader.glsl:3-10 as
+ * run-time parameters.  vrt_uniforms_default() fills in the reference values. */
+typedef struct vrt_uniforms {
+    float camPos[3];           /* uniform vec3 camPos                                */
+    float camRotation[2];      /* uniform vec2 camRotation (declared, unused by the shader) */
+    float lightPos[3];         /* uniform vec3 lightPos: global light, a POINT position */
+    float aspectRatio;         /* uniform float aspectRatio (width/height)          */
+    float rotateMatrix[16];    /* uniform mat4 rotateMatrix, column-major (glUniformMatrix4fv, GL_FALSE) */
+    int32_t viewDepthField;    /* uniform int viewDepthField: 1 = step-count view    */
+    float localLights[VRT_MAX_LOCAL_LIGHTS][4]; /* uniform vec4 localLights[16]: xyz, w = intensity;
+                                                   a light is active iff x,y,z >= 0 */
+    /* ---- extensions; the defaults reproduce the reference exactly ---- */
+    float localLightColor[VRT_MAX_LOCAL_LIGHTS][3]; /* per-channel factor on w; 1,1,1 = reference */
+    float tanHalfFov;          /* tan(vertical fov / 2); 1.0 = the reference's 90 degrees */
+    int32_t maxSteps;          /* RENDER_DIST (384): DDA iteration cap of every ray   */
+    float localLightDist;      /* LOCAL_LIGHT_DIST (64): local light radius         */
+    float ambient;             /* AMBIENT (0.4)                                     */
+    float diffuse;             /* DIFFUSE (0.8)                                     */
+    float maxOverbright;       /* MAX_OVERBRIGHT (1.25)                             */
+} vrt_uniforms;
+
+/* Optional per-pixel side outputs (device pointers, each may be NULL). */
+typedef struct vrt_debug_out {
+    int32_t* hit_index;     /* primary-ray hit voxel index, -1 on a miss            */
+    uint32_t* cast_mask;    /* bit 0: global shadow ray cast; bit 1+i: local light i cast */
+    uint32_t* occ_mask;     /* same bits: set when that shadow ray was blocked      */
+    int32_t* steps;         /* DDA iterations summed over every ray of the pixel    */
+    int32_t* primary_steps; /* DDA iterations of the primary ray (stepCount after castRay #1) */
+    float* shade;           /* 3 floats per pixel: the final light multiplier (r,g,b) */
+} vrt_debug_out;
+
+/* Optional device counters accumulated by a render (8 x uint64, device memory,
+ * caller zeroes): [0] rays cast, [1] DDA iterations, [2] primary hits, [3] pixels. */
+#define VRT_STAT_RAYS 0
+#define VRT_STAT_STEPS 1
+#define VRT_STAT_HITS 2
+#define VRT_STAT_PIXELS 3
+#define VRT_STAT_COUNT 8
+
+/* Render kernel choice. AUTO picks the occupancy-mask kernel unless the world holds
+ * depth-field words, which only the word kernel follows. */
+#define VRT_KERNEL_AUTO 0
+#define VRT_KERNEL_WORD 1     /* one thread per pixel, one 4-byte word per DDA step */
+#define VRT_KERNEL_BITMASK 2  /* occupancy-mask traversal, persistent ray refill    */
+
+typedef struct vrt_render_opts {
+    int32_t kernel;          /* VRT_KERNEL_*                                        */
+    int32_t tile_w, tile_h;  /* ray tile of the mask kernel (0 = default 8x4)       */
+    int32_t refill_min;      /* mask kernel: refill idle lanes once this many are idle (0 = default) */
+    int32_t blocks_per_sm;   /* mask kernel: resident CTAs per SM (0 = default)     */
+} vrt_render_opts;
+
+typedef struct vrt_world vrt_world;
+typedef struct vrt_renderer vrt_renderer;
+
+typedef struct vrt_world_info {
+    int32_t width, height;          /* VOXELS_WIDTH (x and z), VOXELS_HEIGHT (y)      */
+    uint64_t num_words;             /* W*H*W                                          */
+    const int32_t* d_words;         /* device voxel words                             */
+    const uint64_t* d_brick_mask;   /* device occupancy mask: one uint64 per 4x4x4 brick */
+    const uint64_t* d_region_mask;  /* device: one uint64 per 16x16x16 region, bit per brick */
+    int32_t has_depth_field;        /* 1 if any word is < -1 (as of the last sync)    */
+    uint64_t device_bytes;          /* device memory held by the world                */
+} vrt_world_info;
+
+const char* vrt_last_error(void);
+const char* vrt_version(void);
+
+/* ---- uniforms (host only, no GPU) ---- */
+/* Reference constants (fshader.glsl:3-10), identity rotateMatrix, camPos (195,55,155)
+ * (main.cpp:26), aspect 800/600 (main.cpp:11-12,36), lights cleared as initLocalLights. */
+int vrt_uniforms_default(vrt_uniforms* u);
+/* initLocalLights, render.cpp:304-311: every slot (-1,-1,-1,0), colour (1,1,1). */
+int vrt_init_local_lights(vrt_uniforms* u);
+/* placeLocalLight, render.cpp:375-385: the first slot with any coordinate < 0 takes
+ * (x,y,z,a).  Returns the slot used (0..15), or VRT_MAX_LOCAL_LIGHTS when all 16 are
+ * taken, which the reference also ignores silently. */
+int vrt_place_local_light(vrt_uniforms* u, float x, float y, float z, float a);
+/* Camera matrix R_y(yaw) * R_x(pitch) (controls.cpp:136-142), angles in radians,
+ * column-major into m[16]. */
+int vrt_rotate_matrix(float pitch_x, float yaw_y, float* m16);
+
+/* ---- worlds ---- */
+/* A W x H x W world of air (-1) on the current device.  W,H in [1, 65536], W*H*W <= 2^31. */
+int vrt_world_create(int32_t width, int32_t height, vrt_world** out);
+int vrt_world_destroy(vrt_world* w);
+int vrt_world_get_info(const vrt_world* w, vrt_world_info* out);
+/* glBufferData / glBufferSubData (render.cpp:199-202, :219): copy count words from
+ * host memory into words [first, first+count), then refresh the occupancy mask of the
+ * bricks touched and read back the depth-field flag (synchronises the stream).
+ * Pageable or pinned host memory. */
+int vrt_world_upload(vrt_world* w, const int32_t* host_words, uint64_t first, uint64_t count, void* stream);
+/* Same from device memory. */
+int vrt_world_upload_device(vrt_world* w, const int32_t* d_words, uint64_t first, uint64_t count, void* stream);
+/* Copy words [first, first+count) back to host memory. */
+int vrt_world_download(const vrt_world* w, int32_t* host_words, uint64_t first, uint64_t count, void* stream);
+/* Copy the occupancy hierarchy to host memory (any pointer may be NULL): bricks hold
+ * 64*64*SW*SH*SW words, regions 64*SW*SH*SW, supers SW*SH*SW, with SW = ceil(W/64),
+ * SH = ceil(H/64); layout as in vrt_world_info.  Synchronises the stream. */
+int vrt_world_download_masks(const vrt_world* w, uint64_t* bricks, uint64_t* regions, uint64_t* supers,
+                             void* stream);
+/* Recompute has_depth_field (a device reduction; synchronises the stream). */
+int vrt_world_sync_flags(vrt_world* w, void* stream);
+
+/* ---- edits (device scatter) ---- */
+/* removeSphere, level.cpp:30-56: every voxel (cx+x, cy+y, cz+z) with x,y,z in [-r, r),
+ * x*x+y*y+z*z < r*r and inside the world becomes air (-1); the occupancy mask follows.
+ * If refresh_depth_field != 0 the depth field is then recomputed, as the reference does,
+ * for the voxels of the radius r+3 sphere (render.cpp:226-253). r in [0, 1024]. */
+int vrt_remove_sphere(vrt_world* w, int32_t cx, int32_t cy, int32_t cz, int32_t radius,
+                      int32_t refresh_depth_field, void* stream);
+/* placeVoxel, render.cpp:256-262: set one word (ignored outside the world). */
+int vrt_place_voxel(vrt_world* w, int32_t x, int32_t y, int32_t z, int32_t word, void* stream);
+/* fixDepthField, render.cpp:226-253, over every voxel of the box [x0,x1)x[y0,y1)x[z0,z1)
+ * (clipped to the world).  The whole world: 0,0,0,W,H,W. */
+int vrt_fix_depth_field_box(vrt_world* w, int32_t x0, int32_t y0, int32_t z0,
+                            int32_t x1, int32_t y1, int32_t z1, void* stream);
+
+/* ---- world generation ---- */
+/* initVoxels, level.cpp:82-138 (stone/dirt/grass layers and trees, including the
+ * reference's relative-coordinate destroyVoxel calls), run on the device.  The world
+ * must be 512 x 96 x 512, the size level.cpp is written for.  Depth field not included:
+ * call vrt_fix_depth_field_box over the whole world for the app's init state. */
+int vrt_world_init_reference(vrt_world* w, void* stream);
+/* Seeded terrain of the benchmark scenes (host, multi-threaded, deterministic across
+ * CPUs): 2-octave value-noise heightfield in [8,40], grass/dirt/stone bands with +-8
+ * colour jitter, caves where 3-D value noise > 0.7.  Solid = 0x01000000|rgb, air = -1.
+ * Writes W*H*W words to host memory. */
+int vrt_terrain_generate(int32_t* host_words, int32_t width, int32_t height, uint64_t seed, int32_t threads);
+/* Height of column (x,z) of that terrain (first air y above the surface). */
+int vrt_terrain_height(int32_t width, uint64_t seed, int32_t x, int32_t z);
+
+/* ---- rendering ---- */
+/* A renderer owns the device scratch of the persistent kernels (work counters,
+ * counters, host staging).  One renderer per concurrently used stream. */
+int vrt_renderer_create(vrt_renderer** out);
+int vrt_renderer_destroy(vrt_renderer* r);
+
+/* One frame: glDrawArrays(GL_TRIANGLES,0,6) over the fullscreen quad (main.cpp:59) with
+ * the uniforms of render.cpp:289-296.  d_rgba: width*height*4 bytes, row 0 = bottom row
+ * (GL order); pixel (px,py) sees vPos = ((2px+1)/width-1, (2py+1)/height-1).  dbg,
+ * d_stats and opts may be NULL. */
+int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
+               int32_t height, uint8_t* d_rgba, const vrt_debug_out* dbg, uint64_t* d_stats,
+               const vrt_render_opts* opts, void* stream);
+/* vrt_render into the renderer's staging buffer, then copy the image to host memory
+ * (pinned for overlap).  Waits for the stream before returning. */
+int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
+                       int32_t height, uint8_t* host_rgba, const vrt_render_opts* opts, void* stream);
+
+/* One camera of a batch. */
+typedef struct vrt_view {
+    const vrt_world* world;
+    vrt_uniforms uniforms;
+    int32_t width, height;
+    uint8_t* d_rgba;        /* width*height*4 device bytes */
+    uint64_t* d_stats;      /* optional, as vrt_render     */
+} vrt_view;
+
+/* Many cameras (uneven sizes, possibly different worlds without depth fields) in one
+ * persistent launch of the occupancy-mask kernel; tiles are handed out dynamically. */
+int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count,
+                     const vrt_render_opts* opts, void* stream);
+
+/* A captured CUDA graph of vrt_render_batch over a fixed view list; replay with
+ * vrt_batch_graph_launch.  Uniform or image-pointer changes need a new graph. */
+typedef struct vrt_batch_graph vrt_batch_graph;
+int vrt_batch_graph_create(vrt_renderer* r, const vrt_view* views, int32_t count,
+                           const vrt_render_opts* opts, void* stream, vrt_batch_graph** out);
+int vrt_batch_graph_launch(vrt_batch_graph* g, void* stream);
+int vrt_batch_graph_destroy(vrt_batch_graph* g);
+
+/* ---- serving ---- */
+typedef struct vrt_server vrt_server;
+typedef struct vrt_server_config {
+    uint64_t memory_budget_bytes;   /* device bytes the server may hold for images (40 GiB) */
+    int32_t slots;                  /* concurrent batches in flight (streams)          */
+    int32_t max_batch;              /* requests per launch                            */
+    int32_t max_wait_us;            /* how long a partial batch may wait for company   */
+} vrt_server_config;
+
+#define VRT_REQ_RENDER 0
+#define VRT_REQ_EDIT 1
+
+typedef struct vrt_request {
+    int32_t kind;                   /* VRT_REQ_RENDER or VRT_REQ_EDIT                  */
+    int32_t world_id;
+    vrt_uniforms uniforms;          /* render                                         */
+    int32_t width, height;          /* render                                         */
+    uint8_t* host_rgba;             /* render: result destination (host), may be NULL */
+    int32_t cx, cy, cz, radius;     /* edit: removeSphere                             */
+    uint64_t user_tag;
+} vrt_request;
+
+typedef struct vrt_completion {
+    uint64_t user_tag;
+    int32_t status;                 /* 0 ok, VRT_EBUDGET when refused                 */
+    int32_t kind;
+    double submit_ms, start_ms, done_ms; /* server clock: arrival, launch, result ready */
+    uint64_t rays;                  /* rays cast (render)                              */
+} vrt_completion;
+
+int vrt_server_create(const vrt_server_config* cfg, vrt_server** out);
+int vrt_server_destroy(vrt_server* s);
+/* Register a resident world (not owned).  Returns its id in *id. */
+int vrt_server_add_world(vrt_server* s, vrt_world* w, int32_t* id);
+/* Enqueue a request (thread-safe).  Edits of a world run after every earlier render of
+ * that world and before every later one. */
+int vrt_server_submit(vrt_server* s, const vrt_request* req);
+/* Drive the server: admit, batch and launch queued requests, retire finished ones.
+ * Returns the number of completions written to out (up to max_out). */
+int vrt_server_poll(vrt_server* s, vrt_completion* out, int32_t max_out);
+/* Run until every submitted request has completed (completions are kept for poll). */
+int vrt_server_drain(vrt_server* s);
+double vrt_server_now_ms(const vrt_server* s);
+
+/* ---- measurement helpers ---- */
+/* Sustained L2 read bandwidth in GB/s over a resident buffer of the given size. */
+int vrt_probe_l2_read_gbs(uint64_t bytes, int32_t iters, double* gbs_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VRT_H */

@@ -1,0 +1,159 @@
+"""Shared test helpers: golden loading, GPU rendering through the C ABI, comparisons."""
+from __future__ import annotations
+
+import json
+import os
+
+import numpy as np
+
+import vrt
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+# The bar for the shader outputs.  Integer/index work is bit-exact; the north-star
+# floating-point bar is RGB within 1/255 per channel, and this build is held to
+# exact equality of the light multipliers and of the RGBA8 bytes as well.
+RGB_TOL = 1
+
+
+def load_golden(name: str):
+    if name.endswith(".json"):
+        with open(os.path.join(GOLDEN, name)) as f:
+            return json.load(f)
+    return dict(np.load(os.path.join(GOLDEN, name)))
+
+
+def uniforms_from_dict(d: dict) -> vrt.Uniforms:
+    u = vrt.default_uniforms()
+    u.camPos[:] = d["camPos"]
+    u.lightPos[:] = d["lightPos"]
+    u.aspectRatio = d["aspectRatio"]
+    u.rotateMatrix[:] = d["rotateMatrix"]
+    for i in range(16):
+        u.localLights[i][:] = d["localLights"][i]
+    u.maxSteps = d["maxSteps"]
+    u.localLightDist = d["localLightDist"]
+    return u
+
+
+def fcolor_from_outputs(words, hit, shade, primary_steps=None, depth_view=False):
+    """fColor (fshader.glsl:133,144,184-187) rebuilt from hit index and multipliers."""
+    hit = np.asarray(hit)
+    word = words[np.maximum(hit, 0)]
+    ch = np.stack([(word >> 16) & 255, (word >> 8) & 255, word & 255], -1).astype(np.float32)
+    col = (ch / np.float32(255.0)) * shade.astype(np.float32)
+    col[hit < 0] = np.array([0.6, 0.7, 0.8], np.float32)
+    return col
+
+
+def gpu_render(world: vrt.World, u: vrt.Uniforms, width: int, height: int, kernel: int = vrt.KERNEL_AUTO,
+               tile=None, refill_min: int = 0, renderer: vrt.Renderer | None = None):
+    """Render through the C ABI with every debug output; returns numpy arrays + stats."""
+    import torch
+    dev = torch.device("cuda")
+    n = width * height
+    rgba = torch.zeros(n * 4, dtype=torch.uint8, device=dev)
+    hit = torch.full((n,), -7, dtype=torch.int32, device=dev)
+    cast = torch.zeros(n, dtype=torch.int32, device=dev)
+    occ = torch.zeros(n, dtype=torch.int32, device=dev)
+    steps = torch.zeros(n, dtype=torch.int32, device=dev)
+    psteps = torch.zeros(n, dtype=torch.int32, device=dev)
+    shade = torch.zeros(n * 3, dtype=torch.float32, device=dev)
+    stats = torch.zeros(vrt.STAT_COUNT, dtype=torch.int64, device=dev)
+    dbg = vrt.DebugOut(hit.data_ptr(), cast.data_ptr(), occ.data_ptr(), steps.data_ptr(), psteps.data_ptr(),
+                       shade.data_ptr())
+    opts = vrt.RenderOpts()
+    opts.kernel = kernel
+    if tile:
+        opts.tile_w, opts.tile_h = tile
+    opts.refill_min = refill_min
+    r = renderer or vrt.Renderer()
+    stream = torch.cuda.current_stream().cuda_stream
+    r.render(world, u, width, height, rgba.data_ptr(), dbg, stats.data_ptr(), opts, stream)
+    torch.cuda.synchronize()
+    return {
+        "rgba": rgba.cpu().numpy().reshape(height, width, 4),
+        "hit": hit.cpu().numpy().reshape(height, width),
+        "cast": cast.cpu().numpy().view(np.uint32).reshape(height, width),
+        "occ": occ.cpu().numpy().view(np.uint32).reshape(height, width),
+        "steps": steps.cpu().numpy().reshape(height, width),
+        "primary_steps": psteps.cpu().numpy().reshape(height, width),
+        "shade": shade.cpu().numpy().reshape(height, width, 3),
+        "stats": stats.cpu().numpy().astype(np.uint64),
+    }
+
+
+def assert_same_frame(o: dict, g: dict, rows=None):
+    """Oracle vs GPU: hit index, cast/occlusion bits and step counts bit-exact; light
+    multipliers bit-exact; RGBA8 within RGB_TOL (and in practice equal)."""
+    sel = slice(None) if rows is None else rows
+    for key in ("hit", "cast", "occ", "steps", "primary_steps"):
+        a, b = np.asarray(o[key])[sel], np.asarray(g[key])[sel]
+        bad = np.argwhere(a != b)
+        assert bad.size == 0, f"{key}: {len(bad)} mismatches, first at {bad[:3].tolist()}: {a[tuple(bad[0])]} vs {b[tuple(bad[0])]}"
+    a = np.asarray(o["shade"])[sel].view(np.uint32)
+    b = np.asarray(g["shade"])[sel].view(np.uint32)
+    assert np.array_equal(a, b), f"shade: {(a != b).any(-1).sum()} pixels differ"
+    da = np.abs(np.asarray(o["rgba"])[sel].astype(np.int32) - np.asarray(g["rgba"])[sel].astype(np.int32))
+    assert da.max(initial=0) <= RGB_TOL, f"rgba differs by {da.max()}"
+    assert np.array_equal(np.asarray(o["rgba"])[sel], np.asarray(g["rgba"])[sel])
+
+
+def make_world(words: np.ndarray, W: int, H: int) -> vrt.World:
+    w = vrt.World(W, H)
+    w.upload(np.ascontiguousarray(words, np.int32))
+    return w
+
+
+_W64 = (np.uint64(1) << np.arange(64, dtype=np.uint64)).reshape(4, 4, 4)  # [dz][dy][dx] -> bit dx+4dy+16dz
+
+
+def _pack(cells):
+    """cells [..., 4(z), 4(y), 4(x)] bool -> uint64 with bit x + 4y + 16z."""
+    return (cells.astype(np.uint64) * _W64).sum(axis=(-3, -2, -1), dtype=np.uint64)
+
+
+def expected_masks(words, W, H):
+    """The occupancy hierarchy of a world, in the device's storage order:
+    supers[sx + SW*(sy + SH*sz)], regions[super*64 + local], bricks[region*64 + local],
+    local = x + 4y + 16z of the child inside its parent, voxel bit x + 4y + 16z."""
+    SW, SH = (W + 63) // 64, (H + 63) // 64
+    PW, PH = 64 * SW, 64 * SH
+    solid = np.zeros((PW, PH, PW), bool)  # [z][y][x]
+    solid[:W, :H, :W] = words.reshape(W, H, W) >= 0
+    B = _pack(solid.reshape(PW // 4, 4, PH // 4, 4, PW // 4, 4).transpose(0, 2, 4, 1, 3, 5))  # [bz][by][bx]
+    R = _pack((B != 0).reshape(PW // 16, 4, PH // 16, 4, PW // 16, 4).transpose(0, 2, 4, 1, 3, 5))
+    S = _pack((R != 0).reshape(SW, 4, SH, 4, SW, 4).transpose(0, 2, 4, 1, 3, 5))
+    supers = S.reshape(-1)
+    regions = R.reshape(SW, 4, SH, 4, SW, 4).transpose(0, 2, 4, 1, 3, 5).reshape(-1)
+    bricks = B.reshape(SW, 4, 4, SH, 4, 4, SW, 4, 4).transpose(0, 3, 6, 1, 4, 7, 2, 5, 8).reshape(-1)
+    return bricks, regions, supers
+
+
+def expected_masks_loops(words, W, H):
+    """Slow loop form of expected_masks, for checking it on tiny worlds."""
+    SW, SH = (W + 63) // 64, (H + 63) // 64
+    bricks = np.zeros(64 * 64 * SW * SH * SW, np.uint64)
+    for z in range(W):
+        for y in range(H):
+            for x in range(W):
+                if words[x + W * y + W * H * z] < 0:
+                    continue
+                bx, by, bz = x >> 2, y >> 2, z >> 2
+                rx, ry, rz = bx >> 2, by >> 2, bz >> 2
+                sx, sy, sz = rx >> 2, ry >> 2, rz >> 2
+                si = sx + SW * (sy + SH * sz)
+                ri = si * 64 + (rx & 3) + 4 * (ry & 3) + 16 * (rz & 3)
+                bi = ri * 64 + (bx & 3) + 4 * (by & 3) + 16 * (bz & 3)
+                bricks[bi] |= np.uint64(1) << np.uint64((x & 3) + 4 * (y & 3) + 16 * (z & 3))
+    regions = np.zeros(64 * SW * SH * SW, np.uint64)
+    for i in range(regions.size):
+        for c in range(64):
+            if bricks[i * 64 + c]:
+                regions[i] |= np.uint64(1) << np.uint64(c)
+    supers = np.zeros(SW * SH * SW, np.uint64)
+    for i in range(supers.size):
+        for c in range(64):
+            if regions[i * 64 + c]:
+                supers[i] |= np.uint64(1) << np.uint64(c)
+    return bricks, regions, supers

@@ -1,0 +1,83 @@
+"""Batched rendering: many cameras of uneven size in one persistent launch, and the
+same launch captured in a CUDA graph, are bit-identical to one render per camera."""
+import numpy as np
+import pytest
+
+import scenes
+import vrt
+from helpers import gpu_render, make_world
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def batch_setup():
+    sc = scenes.full(2, W=256, H=128, width=64, height=64, max_steps=512)
+    views = scenes.batch_views(sc, 24, seed=7)
+    # scale the sizes down so the per-camera references stay quick
+    views = [(u, max(8, w // 4), max(6, h // 4)) for (u, w, h) in views]
+    for (u, w, h) in views:
+        u.aspectRatio = w / h
+    return sc, views
+
+
+def _batch(torch, renderer, world, views, opts=None, graph=False):
+    imgs = [torch.zeros(w * h * 4, dtype=torch.uint8, device="cuda") for (_, w, h) in views]
+    stats = torch.zeros((len(views), vrt.STAT_COUNT), dtype=torch.int64, device="cuda")
+    vv = [vrt.make_view(world, u, w, h, img.data_ptr(), stats[i].data_ptr())
+          for i, ((u, w, h), img) in enumerate(zip(views, imgs))]
+    stream = torch.cuda.current_stream().cuda_stream
+    if graph:
+        import ctypes as C
+        arr = (vrt.View * len(vv))(*vv)
+        g = C.c_void_p()
+        vrt.check(vrt.lib().vrt_batch_graph_create(renderer.handle, arr, len(vv), C.byref(opts) if opts else None,
+                                                   stream, C.byref(g)))
+        for _ in range(3):
+            stats.zero_()
+            vrt.check(vrt.lib().vrt_batch_graph_launch(g, stream))
+        torch.cuda.synchronize()
+        vrt.lib().vrt_batch_graph_destroy(g)
+    else:
+        renderer.render_batch(vv, opts, stream)
+        torch.cuda.synchronize()
+    return [i.cpu().numpy() for i in imgs], stats.cpu().numpy()
+
+
+def test_batch_equals_single_renders(cuda, batch_setup):
+    sc, views = batch_setup
+    w = make_world(sc.words, sc.W, sc.H)
+    r = vrt.Renderer()
+    imgs, stats = _batch(cuda, r, w, views)
+    for i, (u, width, height) in enumerate(views):
+        g = gpu_render(w, u, width, height, kernel=vrt.KERNEL_WORD)
+        assert np.array_equal(imgs[i].reshape(height, width, 4), g["rgba"]), f"view {i}"
+        assert int(stats[i, vrt.STAT_RAYS]) == int(g["stats"][vrt.STAT_RAYS])
+        assert int(stats[i, vrt.STAT_STEPS]) == int(g["stats"][vrt.STAT_STEPS])
+
+
+@pytest.mark.parametrize("tile,refill", [((16, 8), 4), ((32, 1), 16), ((8, 8), 32)])
+def test_batch_tilings_and_graph(cuda, batch_setup, tile, refill):
+    sc, views = batch_setup
+    w = make_world(sc.words, sc.W, sc.H)
+    r = vrt.Renderer()
+    base, bstats = _batch(cuda, r, w, views)
+    opts = vrt.RenderOpts()
+    opts.kernel = vrt.KERNEL_BITMASK
+    opts.tile_w, opts.tile_h = tile
+    opts.refill_min = refill
+    got, gstats = _batch(cuda, r, w, views, opts, graph=True)
+    for a, b in zip(base, got):
+        assert np.array_equal(a, b)
+    assert np.array_equal(bstats, gstats)
+
+
+def test_batch_rejects_mixed_worlds(cuda, batch_setup):
+    sc, views = batch_setup
+    w1 = make_world(sc.words, sc.W, sc.H)
+    w2 = make_world(sc.words, sc.W, sc.H)
+    r = vrt.Renderer()
+    img = cuda.zeros(64 * 64 * 4, dtype=cuda.uint8, device="cuda")
+    vv = [vrt.make_view(w1, views[0][0], 8, 8, img.data_ptr()), vrt.make_view(w2, views[1][0], 8, 8, img.data_ptr())]
+    with pytest.raises(vrt.VrtError):
+        r.render_batch(vv)

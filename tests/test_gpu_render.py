@@ -1,0 +1,189 @@
+"""Parity of the CUDA render kernels (through the C ABI) with the CPU oracle: hit voxel,
+cast and occlusion bits and DDA step counts bit-exact, light multipliers bit-exact,
+RGBA8 equal (the spec bar is RGB within 1/255)."""
+import numpy as np
+import pytest
+
+import scenes
+import vrt
+from helpers import assert_same_frame, gpu_render, load_golden, make_world, fcolor_from_outputs
+
+pytestmark = pytest.mark.gpu
+
+KERNELS = [vrt.KERNEL_WORD, vrt.KERNEL_BITMASK]
+
+
+@pytest.fixture(scope="module")
+def small():
+    return scenes.small(1)
+
+
+@pytest.fixture(scope="module")
+def full_world():
+    sc = scenes.full(2)
+    return sc
+
+
+def _totals_match(o, g):
+    t = o["totals"]
+    s = g["stats"]
+    assert int(s[vrt.STAT_RAYS]) == t["rays"]
+    assert int(s[vrt.STAT_STEPS]) == t["steps"]
+    assert int(s[vrt.STAT_HITS]) == t["hits"]
+    assert int(s[vrt.STAT_PIXELS]) == t["pixels"]
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_small_scene(cuda, oracle, small, kernel):
+    sc = small
+    o = oracle.render(sc.words, sc.W, sc.H, sc.uniforms, sc.width, sc.height)
+    w = make_world(sc.words, sc.W, sc.H)
+    g = gpu_render(w, sc.uniforms, sc.width, sc.height, kernel=kernel)
+    assert_same_frame(o, g)
+    _totals_match(o, g)
+    assert (o["hit"] >= 0).mean() > 0.2 and (o["occ"] != 0).sum() > 0
+
+
+@pytest.mark.parametrize("seed", [11, 12, 13])
+def test_small_scene_seeds(cuda, oracle, seed):
+    sc = scenes.small(seed)
+    u = sc.uniforms
+    u.aspectRatio = 160 / 120
+    o = oracle.render(sc.words, sc.W, sc.H, u, 160, 120)
+    w = make_world(sc.words, sc.W, sc.H)
+    for k in KERNELS:
+        assert_same_frame(o, gpu_render(w, u, 160, 120, kernel=k))
+
+
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_full_world_reduced_frame(cuda, oracle, full_world, kernel):
+    """512x256x512 world, 16 coloured local lights, 1024 steps, at 480x270."""
+    sc = full_world
+    u = sc.uniforms
+    o = oracle.render(sc.words, sc.W, sc.H, u, 480, 270)
+    w = make_world(sc.words, sc.W, sc.H)
+    g = gpu_render(w, u, 480, 270, kernel=kernel)
+    assert_same_frame(o, g)
+    _totals_match(o, g)
+    assert (o["cast"] > 1).sum() > 0  # local lights are cast
+
+
+def test_full_world_1080p_rows(cuda, oracle, full_world):
+    """The full 1920x1080 frame on the GPU; every 24th row checked against the oracle."""
+    sc = full_world
+    o = oracle.render(sc.words, sc.W, sc.H, sc.uniforms, 1920, 1080, rows=(5, 1080, 24))
+    w = make_world(sc.words, sc.W, sc.H)
+    g = gpu_render(w, sc.uniforms, 1920, 1080, kernel=vrt.KERNEL_BITMASK)
+    assert_same_frame(o, g, rows=slice(5, 1080, 24))
+    g2 = gpu_render(w, sc.uniforms, 1920, 1080, kernel=vrt.KERNEL_WORD)
+    for key in ("rgba", "hit", "cast", "occ", "steps"):
+        assert np.array_equal(g[key], g2[key]), key
+
+
+def test_reference_scene_with_depth_field(cuda, oracle):
+    """The reference world (initVoxels + fixDepthField, built on the device), the word
+    kernel against the reference shader's own golden outputs and the oracle."""
+    gold = load_golden("reference_world.json")
+    case = load_golden("shader_reference_scene.npz")
+    w = vrt.World(512, 96)
+    w.init_reference()
+    w.fix_depth_field()
+    words = w.download(np.empty(512 * 96 * 512, np.int32))
+    import hashlib
+    assert hashlib.sha256(words.tobytes()).hexdigest() == gold["depth_field"]["sha256"]
+    assert w.info().has_depth_field == 1
+    import json
+    from helpers import uniforms_from_dict
+    u = uniforms_from_dict(json.loads(str(case["uniforms"])))
+    g = gpu_render(w, u, 800, 600)  # AUTO picks the word kernel for a depth-field world
+    px, py = case["px"], case["py"]
+    assert np.array_equal(g["hit"][py, px], case["hit"])
+    assert np.array_equal(g["steps"][py, px], case["steps"])
+    col = fcolor_from_outputs(words, g["hit"][py, px], g["shade"][py, px])
+    assert (col.view(np.uint32) == case["color_bits"][:, :3]).all()
+    o = oracle.render(words, 512, 96, u, 800, 600)
+    assert_same_frame(o, g)
+    with pytest.raises(vrt.VrtError) as e:
+        gpu_render(w, u, 64, 48, kernel=vrt.KERNEL_BITMASK)
+    assert e.value.status == vrt.ESTATE
+
+
+def test_reference_world_without_depth_field(cuda, oracle):
+    """The reference world before fixDepthField: both kernels, the reference camera."""
+    w = vrt.World(512, 96)
+    w.init_reference()
+    words = w.download(np.empty(512 * 96 * 512, np.int32))
+    u = scenes.reference_scene_uniforms(-45.0)
+    for i, p in enumerate([(190.0, 45.0, 170.0), (200.0, 44.0, 160.0), (210.0, 50.0, 150.0)]):
+        u.localLights[i][:] = [*p, 0.5]
+    o = oracle.render(words, 512, 96, u, 400, 300)  # default aspect 800/600 == 400/300
+    for k in KERNELS:
+        assert_same_frame(o, gpu_render(w, u, 400, 300, kernel=k))
+
+
+def test_tile_shapes_and_refill_are_invisible(cuda, oracle, small):
+    sc = small
+    o = oracle.render(sc.words, sc.W, sc.H, sc.uniforms, sc.width, sc.height)
+    w = make_world(sc.words, sc.W, sc.H)
+    for tile in [(8, 4), (16, 8), (32, 1), (8, 8), (5, 3)]:
+        for refill in (1, 8, 24, 32):
+            g = gpu_render(w, sc.uniforms, sc.width, sc.height, kernel=vrt.KERNEL_BITMASK, tile=tile,
+                           refill_min=refill)
+            assert_same_frame(o, g)
+
+
+@pytest.mark.parametrize("dims", [(37, 21), (70, 65), (130, 8)])
+def test_odd_world_sizes_random_voxels(cuda, oracle, dims):
+    """World sizes that are not multiples of the brick/region/super sizes, dense noise."""
+    W, H = dims
+    rng = np.random.default_rng(W * 1000 + H)
+    words = np.where(rng.random(W * H * W) < 0.08, 0x01000000 | rng.integers(0, 1 << 24, W * H * W), -1).astype(np.int32)
+    u = vrt.default_uniforms()
+    u.camPos[:] = [W * 0.43, H * 0.61, W * 0.37]
+    u.rotateMatrix[:] = vrt.rotate_matrix(0.3, 2.2)
+    u.lightPos[:] = [W * 0.5, H * 4.0, W * 0.2]
+    u.maxSteps = 3 * W
+    u.localLightDist = float(W)
+    for i in range(5):
+        u.localLights[i][:] = [W * (0.1 + 0.17 * i), H * 0.5, W * (0.8 - 0.13 * i), 0.3]
+    u.aspectRatio = 97 / 61
+    o = oracle.render(words, W, H, u, 97, 61)
+    w = make_world(words, W, H)
+    for k in KERNELS:
+        assert_same_frame(o, gpu_render(w, u, 97, 61, kernel=k))
+
+
+def test_empty_and_full_worlds(cuda, oracle):
+    for fill in (-1, 0x01ABCDEF):
+        words = np.full(64 * 64 * 64, fill, np.int32)
+        u = vrt.default_uniforms()
+        u.camPos[:] = [30.5, 20.5, 10.5]
+        u.maxSteps = 100
+        o = oracle.render(words, 64, 64, u, 33, 17)
+        w = make_world(words, 64, 64)
+        for k in KERNELS:
+            assert_same_frame(o, gpu_render(w, u, 33, 17, kernel=k))
+
+
+def test_render_to_host(cuda, small):
+    sc = small
+    w = make_world(sc.words, sc.W, sc.H)
+    g = gpu_render(w, sc.uniforms, sc.width, sc.height)
+    r = vrt.Renderer()
+    host = np.zeros(sc.width * sc.height * 4, np.uint8)
+    r.render_to_host(w, sc.uniforms, sc.width, sc.height, host.ctypes.data)
+    assert np.array_equal(host.reshape(sc.height, sc.width, 4), g["rgba"])
+
+
+def test_bad_arguments_fail_loudly(cuda, small):
+    sc = small
+    w = make_world(sc.words, sc.W, sc.H)
+    r = vrt.Renderer()
+    with pytest.raises(vrt.VrtError):
+        r.render(w, sc.uniforms, 0, 10, 1234)
+    with pytest.raises(vrt.VrtError):
+        vrt.World(0, 5)
+    u = vrt.default_uniforms()
+    u.maxSteps = -1
+    with pytest.raises(vrt.VrtError):
+        gpu_render(w, u, 8, 8)

@@ -1,0 +1,140 @@
+"""The request server: each result is the same served alone and in a mix with other
+requests, edits keep their order within a world, and the memory budget refuses what
+cannot fit."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+import scenes
+import vrt
+from helpers import gpu_render, make_world
+
+pytestmark = pytest.mark.gpu
+
+
+def make_server(budget=1 << 30, slots=3, max_batch=4):
+    cfg = vrt.ServerConfig(budget, slots, max_batch, 0)
+    h = C.c_void_p()
+    vrt.check(vrt.lib().vrt_server_create(C.byref(cfg), C.byref(h)))
+    return h
+
+
+def add_world(srv, w):
+    wid = C.c_int32()
+    vrt.check(vrt.lib().vrt_server_add_world(srv, w.handle, C.byref(wid)))
+    return wid.value
+
+
+def submit_render(srv, wid, u, width, height, out, tag):
+    q = vrt.Request()
+    q.kind = vrt.REQ_RENDER
+    q.world_id = wid
+    q.uniforms = u
+    q.width, q.height = width, height
+    q.host_rgba = out.ctypes.data if out is not None else None
+    q.user_tag = tag
+    vrt.check(vrt.lib().vrt_server_submit(srv, C.byref(q)))
+
+
+def submit_edit(srv, wid, c, r, tag):
+    q = vrt.Request()
+    q.kind = vrt.REQ_EDIT
+    q.world_id = wid
+    q.cx, q.cy, q.cz = c
+    q.radius = r
+    q.user_tag = tag
+    vrt.check(vrt.lib().vrt_server_submit(srv, C.byref(q)))
+
+
+def collect(srv, n):
+    buf = (vrt.Completion * 256)()
+    out = []
+    vrt.check(vrt.lib().vrt_server_drain(srv))
+    while True:
+        k = vrt.check(vrt.lib().vrt_server_poll(srv, buf, 256))
+        out += [buf[i] for i in range(k)]
+        if k == 0:
+            break
+    assert len(out) == n
+    return {c.user_tag: c for c in out}
+
+
+@pytest.fixture(scope="module")
+def worlds():
+    a = scenes.full(2, W=128, H=64, width=64, height=64, max_steps=256)
+    b = scenes.small(4)
+    return a, b
+
+
+def test_served_in_mix_equals_alone(cuda, worlds):
+    a, b = worlds
+    wa, wb = make_world(a.words, a.W, a.H), make_world(b.words, b.W, b.H)
+    views = scenes.batch_views(a, 10, seed=9, max_steps=256)
+    views = [(u, w // 8 + 8, h // 8 + 6) for (u, w, h) in views]
+    srv = make_server()
+    ia, ib = add_world(srv, wa), add_world(srv, wb)
+    outs = {}
+    for i, (u, w, h) in enumerate(views):
+        u.aspectRatio = w / h
+        outs[i] = (np.zeros(w * h * 4, np.uint8), wa, u, w, h)
+        submit_render(srv, ia, u, w, h, outs[i][0], i)
+        ub = b.uniforms
+        outs[100 + i] = (np.zeros(96 * 64 * 4, np.uint8), wb, ub, 96, 64)
+        ub2 = vrt.Uniforms.from_buffer_copy(ub)
+        ub2.aspectRatio = 96 / 64
+        outs[100 + i] = (outs[100 + i][0], wb, ub2, 96, 64)
+        submit_render(srv, ib, ub2, 96, 64, outs[100 + i][0], 100 + i)
+    done = collect(srv, len(outs))
+    for tag, (img, world, u, w, h) in outs.items():
+        assert done[tag].status == 0
+        alone = gpu_render(world, u, w, h)
+        assert np.array_equal(img.reshape(h, w, 4), alone["rgba"]), f"request {tag}"
+        assert done[tag].rays == int(alone["stats"][vrt.STAT_RAYS])
+        assert done[tag].done_ms >= done[tag].submit_ms
+    vrt.lib().vrt_server_destroy(srv)
+
+
+def test_edits_are_ordered_within_a_world(cuda, worlds):
+    a, _ = worlds
+    w = make_world(a.words, a.W, a.H)
+    u = vrt.Uniforms.from_buffer_copy(a.uniforms)
+    u.aspectRatio = 1.0
+    cam = [int(v) for v in u.camPos]
+    edit = ((cam[0], cam[1] - 3, cam[2]), 6)
+    before = gpu_render(w, u, 48, 48)["rgba"]
+    w2 = make_world(a.words, a.W, a.H)
+    w2.remove_sphere(*edit[0], edit[1], 0)
+    after = gpu_render(w2, u, 48, 48)["rgba"]
+    assert not np.array_equal(before, after)
+    srv = make_server(slots=4, max_batch=2)
+    wid = add_world(srv, w)
+    imgs = [np.zeros(48 * 48 * 4, np.uint8) for _ in range(6)]
+    for i in range(3):
+        submit_render(srv, wid, u, 48, 48, imgs[i], i)
+    submit_edit(srv, wid, edit[0], edit[1], 50)
+    for i in range(3, 6):
+        submit_render(srv, wid, u, 48, 48, imgs[i], i)
+    done = collect(srv, 7)
+    assert done[50].status == 0
+    for i in range(3):
+        assert np.array_equal(imgs[i].reshape(48, 48, 4), before), f"render {i} saw the edit"
+    for i in range(3, 6):
+        assert np.array_equal(imgs[i].reshape(48, 48, 4), after), f"render {i} missed the edit"
+    vrt.lib().vrt_server_destroy(srv)
+
+
+def test_budget_refuses_oversized_requests(cuda, worlds):
+    _, b = worlds
+    w = make_world(b.words, b.W, b.H)
+    srv = make_server(budget=w.info().device_bytes + 64 * 64 * 4 * 2)
+    wid = add_world(srv, w)
+    small = np.zeros(64 * 64 * 4, np.uint8)
+    submit_render(srv, wid, b.uniforms, 64, 64, small, 1)
+    submit_render(srv, wid, b.uniforms, 640, 480, None, 2)  # larger than the whole budget
+    done = collect(srv, 2)
+    assert done[1].status == 0 and done[2].status == vrt.EBUDGET
+    with pytest.raises(vrt.VrtError):
+        big = make_world(np.full(128 * 64 * 128, -1, np.int32), 128, 64)
+        add_world(srv, big)
+    vrt.lib().vrt_server_destroy(srv)

@@ -1,0 +1,55 @@
+"""Host-side logic that needs no GPU: the occupancy-layout model used by the GPU tests,
+the uniform helpers of the C ABI, and the seeded scene builders."""
+import math
+
+import numpy as np
+
+from helpers import expected_masks, expected_masks_loops
+
+
+def test_mask_layout_model_matches_loops():
+    rng = np.random.default_rng(3)
+    for W, H in [(20, 9), (64, 64), (70, 66)]:
+        words = np.where(rng.random(W * H * W) < 0.01, 5, -1).astype(np.int32)
+        for a, b in zip(expected_masks(words, W, H), expected_masks_loops(words, W, H)):
+            assert np.array_equal(a, b)
+
+
+def test_uniform_defaults_are_the_reference_constants(vrt_lib):
+    u = vrt_lib.default_uniforms()
+    assert u.maxSteps == 384 and u.localLightDist == 64.0            # fshader.glsl:5,7
+    assert np.float32(u.ambient) == np.float32(0.4)                   # :8
+    assert np.float32(u.diffuse) == np.float32(0.8)                   # :9
+    assert np.float32(u.maxOverbright) == np.float32(1.25)            # :10
+    assert list(u.camPos) == [195.0, 55.0, 155.0]                     # main.cpp:26
+    assert u.tanHalfFov == 1.0 and u.viewDepthField == 0
+    assert all(list(u.localLights[i]) == [-1.0, -1.0, -1.0, 0.0] for i in range(16))  # render.cpp:304-311
+    assert list(u.rotateMatrix) == [float(i % 5 == 0) for i in range(16)]
+
+
+def test_place_local_light_fills_then_ignores(vrt_lib):
+    u = vrt_lib.default_uniforms()
+    slots = [vrt_lib.place_local_light(u, float(i), 1.0, 2.0, 0.5) for i in range(18)]
+    assert slots == list(range(16)) + [-1, -1]
+    u.localLights[5][1] = -3.0  # a slot with any negative coordinate is free again
+    assert vrt_lib.place_local_light(u, 9.0, 9.0, 9.0, 0.25) == 5
+
+
+def test_rotate_matrix_convention(vrt_lib):
+    m = np.float32(vrt_lib.rotate_matrix(math.radians(30.0), 0.0)).reshape(4, 4).T  # row-major view
+    d = m[:3, :3] @ np.float32([0.0, 0.0, 1.0])
+    assert d[1] < 0  # positive camRotation.x looks down (controls.cpp:136-142)
+
+
+def test_scenes_are_deterministic(vrt_lib):
+    import scenes
+    a, b = scenes.small(1), scenes.small(1)
+    assert np.array_equal(a.words, b.words)
+    assert bytes(a.uniforms) == bytes(b.uniforms)
+    c = scenes.small(2)
+    assert bytes(a.uniforms) != bytes(c.uniforms)
+    f = scenes.full(2, W=128, H=64, width=64, height=36, max_steps=64)
+    lit = [f.uniforms.localLights[i][0] >= 0 for i in range(16)]
+    assert all(lit)
+    v = scenes.batch_views(f, 8, seed=3)
+    assert len(v) == 8 and all(240 <= h <= 1080 for _, _, h in v)

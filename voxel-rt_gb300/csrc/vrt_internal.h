@@ -1,0 +1,76 @@
+// Internal declarations shared by the translation units of libvrt.so.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <cstdint>
+#include <cstdio>
+#include <string>
+
+#include "../../include/vrt.h"
+
+namespace vrt {
+
+// ---- error plumbing: every C entry point returns a status and records a message ----
+int set_error(int status, const char* fmt, ...);
+int cuda_error(cudaError_t e, const char* what);
+
+#define VRT_CUDA(call)                                       \
+    do {                                                     \
+        cudaError_t e_ = (call);                             \
+        if (e_ != cudaSuccess) return ::vrt::cuda_error(e_, #call); \
+    } while (0)
+
+// ---- occupancy hierarchy ----
+// Three levels of 64-bit masks over the voxel words (a 64-ary tree):
+//   brick  (4x4x4 voxels):   bit (x&3) + 4*(y&3) + 16*(z&3) set when that voxel is solid
+//   region (16x16x16):       bit per brick (bx&3) + 4*(by&3) + 16*(bz&3) set when the brick has a solid voxel
+//   super  (64x64x64):       bit per region, same layout, set when the region has a solid voxel
+// Bricks are stored region-major (64 bricks of a region = 512 contiguous bytes) and
+// regions super-major (64 regions of a super block = 512 bytes), so the nodes a ray
+// visits are close together.  Voxels outside the world count as empty.
+struct Layout {
+    int W, H;           // voxel dims: x,z in [0,W), y in [0,H)
+    int RW, RH;         // regions per axis (x/z, y): ceil(W/16), ceil(H/16)
+    int SW, SH;         // super blocks per axis: ceil(W/64), ceil(H/64)
+    int RWp, RHp;       // regions per axis padded to a multiple of 4 (= 4*SW, 4*SH)
+    uint64_t n_words;   // W*H*W
+    uint64_t n_bricks;  // 64 * RWp*RHp*RWp
+    uint64_t n_regions; // 64 * SW*SH*SW
+    uint64_t n_supers;  // SW*SH*SW
+};
+
+__host__ __device__ inline uint64_t super_index(const Layout& L, int sx, int sy, int sz) {
+    return (uint64_t)sx + (uint64_t)L.SW * ((uint64_t)sy + (uint64_t)L.SH * sz);
+}
+// region (rx,ry,rz) -> slot in the region array
+__host__ __device__ inline uint64_t region_index(const Layout& L, int rx, int ry, int rz) {
+    return super_index(L, rx >> 2, ry >> 2, rz >> 2) * 64 + ((rx & 3) + 4 * (ry & 3) + 16 * (rz & 3));
+}
+// brick (bx,by,bz) -> slot in the brick array
+__host__ __device__ inline uint64_t brick_index(const Layout& L, int bx, int by, int bz) {
+    return region_index(L, bx >> 2, by >> 2, bz >> 2) * 64 + ((bx & 3) + 4 * (by & 3) + 16 * (bz & 3));
+}
+
+Layout make_layout(int W, int H);
+
+}  // namespace vrt
+
+struct vrt_world {
+    vrt::Layout L;
+    int32_t* d_words = nullptr;
+    uint64_t* d_bricks = nullptr;
+    uint64_t* d_regions = nullptr;
+    uint64_t* d_supers = nullptr;
+    int* d_flag = nullptr;          // has-depth-field flag written by the mask kernels
+    int has_depth_field = 0;        // host copy (as of the last sync)
+    uint64_t device_bytes = 0;
+    int device = 0;
+};
+
+namespace vrt {
+// Rebuild the masks of every brick overlapping words [first, first+count).
+int refresh_masks(vrt_world* w, uint64_t first, uint64_t count, cudaStream_t s);
+// Rebuild the masks of the voxel box [x0,x1)x[y0,y1)x[z0,z1) (clipped).
+int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int z1, cudaStream_t s);
+}  // namespace vrt

@@ -1,0 +1,487 @@
+// Device-resident worlds: the voxel words (the reference's SSBO), the derived occupancy
+// hierarchy, and the edit kernels that replace the reference's CPU world code:
+//   removeSphere  level.cpp:30-56        -> remove_sphere_kernel + mask refresh + depth refresh
+//   fixDepthField render.cpp:226-253     -> fix_depth_field_kernel
+//   placeVoxel    render.cpp:256-262     -> place_voxel_kernel
+//   initVoxels    level.cpp:82-138       -> init_reference_layers_kernel + init_reference_trees_kernel
+//   updateGeometry/updatePartialGeometry render.cpp:199-223 -> vrt_world_upload (+ mask refresh)
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstring>
+#include <mutex>
+#include <vector>
+
+#include "vrt_internal.h"
+
+namespace vrt {
+
+Layout make_layout(int W, int H) {
+    Layout L{};
+    L.W = W;
+    L.H = H;
+    L.RW = (W + 15) / 16;
+    L.RH = (H + 15) / 16;
+    L.SW = (W + 63) / 64;
+    L.SH = (H + 63) / 64;
+    L.RWp = 4 * L.SW;
+    L.RHp = 4 * L.SH;
+    L.n_words = (uint64_t)W * H * W;
+    L.n_supers = (uint64_t)L.SW * L.SH * L.SW;
+    L.n_regions = 64 * L.n_supers;
+    L.n_bricks = 64 * L.n_regions;
+    return L;
+}
+
+// ------------------------------------------------------------------ mask kernels
+
+// One thread per brick of the brick box [b0, b1): OR of (word >= 0) over its 4x4x4
+// voxels; any word < -1 raises the depth-field flag.
+__global__ void brick_mask_kernel(const int32_t* __restrict__ words, uint64_t* __restrict__ bricks, int* flag,
+                                  Layout L, int bx0, int by0, int bz0, int nbx, int nby, int nbz) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t total = (uint64_t)nbx * nby * nbz;
+    if (t >= total) return;
+    int bx = bx0 + (int)(t % nbx);
+    int by = by0 + (int)((t / nbx) % nby);
+    int bz = bz0 + (int)(t / ((uint64_t)nbx * nby));
+    uint64_t m = 0;
+    bool depth = false;
+    const int x0 = bx * 4;
+    const bool vec = (x0 + 4 <= L.W) && ((L.W & 3) == 0);
+    for (int dz = 0; dz < 4; dz++) {
+        int z = bz * 4 + dz;
+        if (z >= L.W) break;
+        for (int dy = 0; dy < 4; dy++) {
+            int y = by * 4 + dy;
+            if (y >= L.H) break;
+            const int32_t* row = words + ((uint64_t)z * L.H + y) * L.W;
+            int v[4];
+            if (vec) {
+                int4 q = __ldg(reinterpret_cast<const int4*>(row + x0));
+                v[0] = q.x; v[1] = q.y; v[2] = q.z; v[3] = q.w;
+            } else {
+                for (int dx = 0; dx < 4; dx++) v[dx] = (x0 + dx < L.W) ? __ldg(row + x0 + dx) : -1;
+            }
+            for (int dx = 0; dx < 4; dx++) {
+                if (v[dx] >= 0) m |= 1ull << (dx + 4 * dy + 16 * dz);
+                depth |= (v[dx] < -1);
+            }
+        }
+    }
+    bricks[brick_index(L, bx, by, bz)] = m;
+    if (depth) atomicOr(flag, 1);
+}
+
+// One thread per node of the parent box: bit i set when child i is non-zero.
+// children are stored as 64 consecutive uint64 per parent (region-major / super-major).
+__global__ void parent_mask_kernel(const uint64_t* __restrict__ child, uint64_t* __restrict__ parent,
+                                   int px0, int py0, int pz0, int npx, int npy, int npz, Layout L, int level) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    uint64_t total = (uint64_t)npx * npy * npz;
+    if (t >= total) return;
+    int px = px0 + (int)(t % npx);
+    int py = py0 + (int)((t / npx) % npy);
+    int pz = pz0 + (int)(t / ((uint64_t)npx * npy));
+    uint64_t slot = level == 1 ? region_index(L, px, py, pz) : super_index(L, px, py, pz);
+    const uint64_t* c = child + slot * 64;
+    uint64_t m = 0;
+    for (int i = 0; i < 64; i += 2) {
+        ulonglong2 q = *reinterpret_cast<const ulonglong2*>(c + i);
+        m |= (uint64_t)(q.x != 0) << i;
+        m |= (uint64_t)(q.y != 0) << (i + 1);
+    }
+    parent[slot] = m;
+}
+
+static inline unsigned blocks_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
+
+int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int z1, cudaStream_t s) {
+    const Layout& L = w->L;
+    x0 = std::max(x0, 0); y0 = std::max(y0, 0); z0 = std::max(z0, 0);
+    x1 = std::min(x1, L.W); y1 = std::min(y1, L.H); z1 = std::min(z1, L.W);
+    if (x0 >= x1 || y0 >= y1 || z0 >= z1) return VRT_OK;
+    int bx0 = x0 >> 2, by0 = y0 >> 2, bz0 = z0 >> 2;
+    int bx1 = (x1 + 3) >> 2, by1 = (y1 + 3) >> 2, bz1 = (z1 + 3) >> 2;
+    uint64_t nb = (uint64_t)(bx1 - bx0) * (by1 - by0) * (bz1 - bz0);
+    brick_mask_kernel<<<blocks_for(nb, 256), 256, 0, s>>>(w->d_words, w->d_bricks, w->d_flag, L, bx0, by0, bz0,
+                                                           bx1 - bx0, by1 - by0, bz1 - bz0);
+    int rx0 = bx0 >> 2, ry0 = by0 >> 2, rz0 = bz0 >> 2;
+    int rx1 = (bx1 + 3) >> 2, ry1 = (by1 + 3) >> 2, rz1 = (bz1 + 3) >> 2;
+    uint64_t nr = (uint64_t)(rx1 - rx0) * (ry1 - ry0) * (rz1 - rz0);
+    parent_mask_kernel<<<blocks_for(nr, 256), 256, 0, s>>>(w->d_bricks, w->d_regions, rx0, ry0, rz0, rx1 - rx0,
+                                                           ry1 - ry0, rz1 - rz0, L, 1);
+    int sx0 = rx0 >> 2, sy0 = ry0 >> 2, sz0 = rz0 >> 2;
+    int sx1 = (rx1 + 3) >> 2, sy1 = (ry1 + 3) >> 2, sz1 = (rz1 + 3) >> 2;
+    uint64_t ns = (uint64_t)(sx1 - sx0) * (sy1 - sy0) * (sz1 - sz0);
+    parent_mask_kernel<<<blocks_for(ns, 256), 256, 0, s>>>(w->d_regions, w->d_supers, sx0, sy0, sz0, sx1 - sx0,
+                                                           sy1 - sy0, sz1 - sz0, L, 2);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+int refresh_masks(vrt_world* w, uint64_t first, uint64_t count, cudaStream_t s) {
+    if (count == 0) return VRT_OK;
+    const Layout& L = w->L;
+    uint64_t last = first + count - 1;
+    uint64_t plane = (uint64_t)L.W * L.H;
+    int z0 = (int)(first / plane), z1 = (int)(last / plane);
+    if (z0 != z1) return refresh_masks_box(w, 0, 0, z0, L.W, L.H, z1 + 1, s);
+    int y0 = (int)((first % plane) / L.W), y1 = (int)((last % plane) / L.W);
+    if (y0 != y1) return refresh_masks_box(w, 0, y0, z0, L.W, y1 + 1, z0 + 1, s);
+    int x0 = (int)(first % L.W), x1 = (int)(last % L.W);
+    return refresh_masks_box(w, x0, y0, z0, x1 + 1, y0 + 1, z0 + 1, s);
+}
+
+// ------------------------------------------------------------------ edits
+
+// removeSphere's first loop (level.cpp:31-42): voxels with offsets in [-r,r)^3,
+// x*x+y*y+z*z < r*r and inside the world become air.
+__global__ void remove_sphere_kernel(int32_t* __restrict__ words, Layout L, int cx, int cy, int cz, int r) {
+    int n = 2 * r;
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)n * n * n) return;
+    int x = (int)(t % n) - r, y = (int)((t / n) % n) - r, z = (int)(t / ((uint64_t)n * n)) - r;
+    int ax = x + cx, ay = y + cy, az = z + cz;
+    if (ax < L.W && ay < L.H && az < L.W && ax >= 0 && ay >= 0 && az >= 0 && x * x + y * y + z * z < r * r)
+        words[(uint64_t)ax + (uint64_t)L.W * ay + (uint64_t)L.W * L.H * az] = -1;
+}
+
+__global__ void place_voxel_kernel(int32_t* words, Layout L, int x, int y, int z, int32_t v) {
+    if (x >= 0 && y >= 0 && z >= 0 && x < L.W && y < L.H && z < L.W)
+        words[(uint64_t)x + (uint64_t)L.W * y + (uint64_t)L.W * L.H * z] = v;
+}
+
+// Depth-field offsets of computeDepthIndices (render.cpp:66-100), reduced to what
+// fixDepthField (render.cpp:226-253) can use.  fixDepthField keeps, over the solid
+// neighbours in the radius-7 sphere whose shrunk distance d beats the running value
+// (start -6), the value (d <= -2 ? d : 0); the running value only grows and that map
+// is monotone, so the result is g(max d) over solid neighbours with d > -6, whatever
+// the visiting order.  The table therefore holds the sphere offsets with d > -6 sorted
+// by decreasing d, and the kernel stops at the first solid neighbour.
+struct DepthOff {
+    float dist;
+    int8_t x, y, z, pad;
+};
+__constant__ DepthOff c_depth_offs[1024];
+__constant__ int c_depth_count;
+static std::once_flag g_depth_once;
+static int g_depth_count = 0;
+static std::vector<DepthOff> g_depth_table;
+
+static void build_depth_table() {
+    const int R = 7;  // DEPTH_FIELD_RADIUS, render.hpp:7
+    std::vector<DepthOff> v;
+    for (int z = -R; z <= R; z++)
+        for (int y = -R; y <= R; y++)
+            for (int x = -R; x <= R; x++) {
+                if (x * x + y * y + z * z > R * R) continue;
+                int xd = x - (x > 0) + (x < 0), yd = y - (y > 0) + (y < 0), zd = z - (z > 0) + (z < 0);
+                // render.cpp:81: dist = -sqrt(int) through double sqrt, stored as float
+                float dist = (float)(-std::sqrt((double)(xd * xd + yd * yd + zd * zd)));
+                if (dist > (float)(-R + 1)) v.push_back(DepthOff{dist, (int8_t)x, (int8_t)y, (int8_t)z, 0});
+            }
+    std::stable_sort(v.begin(), v.end(), [](const DepthOff& a, const DepthOff& b) { return a.dist > b.dist; });
+    g_depth_table = v;
+    g_depth_count = (int)v.size();
+}
+
+static int ensure_depth_table() {
+    std::call_once(g_depth_once, build_depth_table);
+    // constant memory is per device: upload each time (cheap, 8 KB) to stay correct on any device
+    VRT_CUDA(cudaMemcpyToSymbol(c_depth_offs, g_depth_table.data(), g_depth_table.size() * sizeof(DepthOff)));
+    VRT_CUDA(cudaMemcpyToSymbol(c_depth_count, &g_depth_count, sizeof(int)));
+    return VRT_OK;
+}
+
+// fixDepthField (render.cpp:226-253) for every voxel of the box, or of the sphere
+// x*x+y*y+z*z < r2*r2 around (cx,cy,cz) when r2 > 0 (removeSphere's second loop,
+// level.cpp:43-55).  Neighbours outside the world count as not solid (the reference
+// reads voxels[-1] there).  Only air words are written and only solidity is read, so
+// voxels of one launch do not interact.
+__global__ void fix_depth_field_kernel(int32_t* words, Layout L, int x0, int y0, int z0, int nx,
+                                       int ny, int nz, int cx, int cy, int cz, int r2) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)nx * ny * nz) return;
+    int x = x0 + (int)(t % nx), y = y0 + (int)((t / nx) % ny), z = z0 + (int)(t / ((uint64_t)nx * ny));
+    if (x < 0 || y < 0 || z < 0 || x >= L.W || y >= L.H || z >= L.W) return;
+    if (r2 > 0) {
+        int ox = x - cx, oy = y - cy, oz = z - cz;
+        if (ox * ox + oy * oy + oz * oz >= r2 * r2) return;
+    }
+    uint64_t idx = (uint64_t)x + (uint64_t)L.W * y + (uint64_t)L.W * L.H * z;
+    if (words[idx] >= 0) return;
+    float nearest = -6.0f;  // -DEPTH_FIELD_RADIUS + 1
+    const int n = c_depth_count;
+    for (int i = 0; i < n; i++) {
+        DepthOff o = c_depth_offs[i];
+        int qx = x + o.x, qy = y + o.y, qz = z + o.z;
+        if (qx < 0 || qy < 0 || qz < 0 || qx >= L.W || qy >= L.H || qz >= L.W) continue;
+        // plain load: this launch writes other air words of the same array
+        if (words[(uint64_t)qx + (uint64_t)L.W * qy + (uint64_t)L.W * L.H * qz] >= 0) {
+            nearest = o.dist <= -2.0f ? o.dist : 0.0f;
+            break;
+        }
+    }
+    if (nearest < 0.0f) words[idx] = __float_as_int(nearest);
+}
+
+// ------------------------------------------------------------------ initVoxels
+
+// level.cpp:85-128: stone/dirt/grass layers, then the holes that placeBush/placeTrunk
+// punch near the origin by calling destroyVoxel with relative coordinates
+// (level.cpp:11,64): (0,0..5,0) from the trunks and the x,y,z >= 0 part of the radius-6
+// ball from the bushes.  Both are applied after the layers, as in the reference.
+__global__ void init_reference_layers_kernel(int32_t* __restrict__ words, Layout L, int any_tree) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L.n_words) return;
+    int x = (int)(t % L.W), y = (int)((t / L.W) % L.H), z = (int)(t / ((uint64_t)L.W * L.H));
+    int cv = 5 * ((x + y + z) % 3);
+    int v = -1;
+    if (y <= 25) v = ((90 + cv) << 16) | ((90 + cv) << 8) | (90 + cv);
+    else if (y <= 33) v = ((120 + cv) << 16) | ((100 + cv) << 8);
+    else if (y <= 36) v = (10 << 16) | ((130 + cv) << 8) | 10;
+    if (any_tree) {
+        if (x == 0 && z == 0 && y < 6) v = -1;
+        if (x < 6 && y < 6 && z < 6 && x * x + y * y + z * z < 36) v = -1;
+    }
+    words[t] = v;
+}
+
+// One tree per blockIdx.y: trunk (placeTrunk, level.cpp:59-79) then bush (placeBush,
+// level.cpp:4-27) over the tree's bounding box [-6,6)^3 around the bush centre, which
+// contains the trunk; the bush is written last, so it wins where the two overlap.
+// Trees are 30 x 25 voxels apart and never overlap each other.
+__global__ void init_reference_trees_kernel(int32_t* __restrict__ words, Layout L, int trees_x) {
+    int tree = blockIdx.y;
+    int tx = 30 * (1 + tree % trees_x);       // x % 30 == 0, x in [10, W-10)
+    int tz = 25 * (1 + tree / trees_x);       // z % 25 == 0, z in [10, W-10)
+    int bush_x = tx + tz % 7, bush_y = 46, bush_z = tz;      // level.cpp:134
+    int trunk_x = tx + 1 + tz % 7, trunk_y = 36, trunk_z = tz; // level.cpp:133
+    // box around the bush centre: x in [bush_x-6, bush_x+6) covers the trunk (x offsets [-2,1) from bush_x+1)
+    int t = blockIdx.x * blockDim.x + threadIdx.x;
+    const int bw = 12, bh = 16;  // y from 36 (trunk base) to 52 (bush top)
+    if (t >= bw * bh * bw) return;
+    int ax = bush_x - 6 + t % bw;
+    int ay = 36 + (t / bw) % bh;
+    int az = bush_z - 6 + t / (bw * bh);
+    if (ax < 0 || ay < 0 || az < 0 || ax >= L.W || ay >= L.H || az >= L.W) return;
+    int v = 0;
+    bool write = false;
+    {   // placeTrunk(ivec3(trunk_x, 36, tz), ivec3(128,100,15), 6): x,z in [-2,1), y in [0,6)
+        int x = ax - trunk_x, y = ay - trunk_y, z = az - trunk_z;
+        if (x >= -2 && x < 1 && z >= -2 && z < 1 && y >= 0 && y < 6) {
+            int r = 128 - ((x + z) % 2) * 10, g = 100 - ((x + z) % 2) * 10;
+            v = (((r << 8) + g) << 8) + 15;
+            write = true;
+        }
+    }
+    {   // placeBush(ivec3(bush_x, 46, tz), ivec3(15,128,15), 6): offsets in [-6,6)^3, |o|^2 < 36
+        int x = ax - bush_x, y = ay - bush_y, z = az - bush_z;
+        if (x >= -6 && x < 6 && y >= -6 && y < 6 && z >= -6 && z < 6 && x * x + y * y + z * z < 36) {
+            int g = 128 - ((x + y + z) % 3) * 20;
+            v = (((15 << 8) + g) << 8) + 15;
+            write = true;
+        }
+    }
+    if (write) words[(uint64_t)ax + (uint64_t)L.W * ay + (uint64_t)L.W * L.H * az] = v;
+}
+
+}  // namespace vrt
+
+using namespace vrt;
+
+static inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+extern "C" {
+
+int vrt_world_create(int32_t width, int32_t height, vrt_world** out) {
+    if (!out) return set_error(VRT_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (width < 1 || height < 1 || width > 65536 || height > 65536)
+        return set_error(VRT_EINVAL, "world %d x %d x %d out of range", width, height, width);
+    uint64_t n = (uint64_t)width * height * width;
+    if (n > (1ull << 31)) return set_error(VRT_ERANGE, "world of %llu voxels exceeds 2^31", (unsigned long long)n);
+    vrt_world* w = new vrt_world();
+    w->L = make_layout(width, height);
+    cudaGetDevice(&w->device);
+    uint64_t bytes = w->L.n_words * 4 + (w->L.n_bricks + w->L.n_regions + w->L.n_supers) * 8 + 256;
+    cudaError_t e = cudaMalloc(&w->d_words, w->L.n_words * 4);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_bricks, w->L.n_bricks * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_regions, w->L.n_regions * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_supers, w->L.n_supers * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_flag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(w->d_words, 0xFF, w->L.n_words * 4);  // air = -1 (render.cpp:349-351)
+    if (e == cudaSuccess) e = cudaMemset(w->d_bricks, 0, w->L.n_bricks * 8);
+    if (e == cudaSuccess) e = cudaMemset(w->d_regions, 0, w->L.n_regions * 8);
+    if (e == cudaSuccess) e = cudaMemset(w->d_supers, 0, w->L.n_supers * 8);
+    if (e == cudaSuccess) e = cudaMemset(w->d_flag, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaDeviceSynchronize();
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        vrt_world_destroy(w);
+        return e == cudaErrorMemoryAllocation ? set_error(VRT_ENOMEM, "world allocation: %s", cudaGetErrorString(e))
+                                              : cuda_error(e, "vrt_world_create");
+    }
+    w->device_bytes = bytes;
+    *out = w;
+    return VRT_OK;
+}
+
+int vrt_world_destroy(vrt_world* w) {
+    if (!w) return VRT_OK;
+    cudaFree(w->d_words);
+    cudaFree(w->d_bricks);
+    cudaFree(w->d_regions);
+    cudaFree(w->d_supers);
+    cudaFree(w->d_flag);
+    delete w;
+    return VRT_OK;
+}
+
+int vrt_world_get_info(const vrt_world* w, vrt_world_info* out) {
+    if (!w || !out) return set_error(VRT_EINVAL, "NULL argument");
+    out->width = w->L.W;
+    out->height = w->L.H;
+    out->num_words = w->L.n_words;
+    out->d_words = w->d_words;
+    out->d_brick_mask = w->d_bricks;
+    out->d_region_mask = w->d_regions;
+    out->has_depth_field = w->has_depth_field;
+    out->device_bytes = w->device_bytes;
+    return VRT_OK;
+}
+
+static int upload_common(vrt_world* w, const int32_t* src, uint64_t first, uint64_t count, void* stream,
+                         cudaMemcpyKind kind) {
+    if (!w || (!src && count)) return set_error(VRT_EINVAL, "NULL argument");
+    if (first > w->L.n_words || count > w->L.n_words - first)
+        return set_error(VRT_ERANGE, "words [%llu, %llu) beyond the world's %llu", (unsigned long long)first,
+                         (unsigned long long)(first + count), (unsigned long long)w->L.n_words);
+    if (count == 0) return VRT_OK;
+    VRT_CUDA(cudaMemcpyAsync(w->d_words + first, src, count * 4, kind, S(stream)));
+    int st = refresh_masks(w, first, count, S(stream));
+    if (st) return st;
+    // the kernel choice depends on the depth-field flag: read it back now
+    int flag = 0;
+    VRT_CUDA(cudaMemcpyAsync(&flag, w->d_flag, sizeof(int), cudaMemcpyDeviceToHost, S(stream)));
+    VRT_CUDA(cudaStreamSynchronize(S(stream)));
+    w->has_depth_field |= flag;
+    return VRT_OK;
+}
+
+int vrt_world_upload(vrt_world* w, const int32_t* host_words, uint64_t first, uint64_t count, void* stream) {
+    return upload_common(w, host_words, first, count, stream, cudaMemcpyHostToDevice);
+}
+
+int vrt_world_upload_device(vrt_world* w, const int32_t* d_words, uint64_t first, uint64_t count, void* stream) {
+    return upload_common(w, d_words, first, count, stream, cudaMemcpyDeviceToDevice);
+}
+
+int vrt_world_download(const vrt_world* w, int32_t* host_words, uint64_t first, uint64_t count, void* stream) {
+    if (!w || (!host_words && count)) return set_error(VRT_EINVAL, "NULL argument");
+    if (first > w->L.n_words || count > w->L.n_words - first) return set_error(VRT_ERANGE, "range beyond the world");
+    if (count == 0) return VRT_OK;
+    VRT_CUDA(cudaMemcpyAsync(host_words, w->d_words + first, count * 4, cudaMemcpyDeviceToHost, S(stream)));
+    VRT_CUDA(cudaStreamSynchronize(S(stream)));
+    return VRT_OK;
+}
+
+int vrt_world_download_masks(const vrt_world* w, uint64_t* bricks, uint64_t* regions, uint64_t* supers,
+                             void* stream) {
+    if (!w) return set_error(VRT_EINVAL, "NULL world");
+    if (bricks)
+        VRT_CUDA(cudaMemcpyAsync(bricks, w->d_bricks, w->L.n_bricks * 8, cudaMemcpyDeviceToHost, S(stream)));
+    if (regions)
+        VRT_CUDA(cudaMemcpyAsync(regions, w->d_regions, w->L.n_regions * 8, cudaMemcpyDeviceToHost, S(stream)));
+    if (supers)
+        VRT_CUDA(cudaMemcpyAsync(supers, w->d_supers, w->L.n_supers * 8, cudaMemcpyDeviceToHost, S(stream)));
+    VRT_CUDA(cudaStreamSynchronize(S(stream)));
+    return VRT_OK;
+}
+
+// The flag is raised by the brick kernel whenever it sees a word < -1 and never lowered
+// by it; a full-world refresh after clearing gives the exact current state.
+int vrt_world_sync_flags(vrt_world* w, void* stream) {
+    if (!w) return set_error(VRT_EINVAL, "NULL world");
+    VRT_CUDA(cudaMemsetAsync(w->d_flag, 0, sizeof(int), S(stream)));
+    int st = refresh_masks_box(w, 0, 0, 0, w->L.W, w->L.H, w->L.W, S(stream));
+    if (st) return st;
+    int flag = 0;
+    VRT_CUDA(cudaMemcpyAsync(&flag, w->d_flag, sizeof(int), cudaMemcpyDeviceToHost, S(stream)));
+    VRT_CUDA(cudaStreamSynchronize(S(stream)));
+    w->has_depth_field = flag;
+    return VRT_OK;
+}
+
+int vrt_place_voxel(vrt_world* w, int32_t x, int32_t y, int32_t z, int32_t word, void* stream) {
+    if (!w) return set_error(VRT_EINVAL, "NULL world");
+    if (x < 0 || y < 0 || z < 0 || x >= w->L.W || y >= w->L.H || z >= w->L.W) return VRT_OK;  // render.cpp:259
+    place_voxel_kernel<<<1, 1, 0, S(stream)>>>(w->d_words, w->L, x, y, z, word);
+    VRT_CUDA(cudaGetLastError());
+    if (word < -1) w->has_depth_field = 1;
+    return refresh_masks_box(w, x, y, z, x + 1, y + 1, z + 1, S(stream));
+}
+
+int vrt_fix_depth_field_box(vrt_world* w, int32_t x0, int32_t y0, int32_t z0, int32_t x1, int32_t y1, int32_t z1,
+                            void* stream) {
+    if (!w) return set_error(VRT_EINVAL, "NULL world");
+    x0 = std::max(x0, 0); y0 = std::max(y0, 0); z0 = std::max(z0, 0);
+    x1 = std::min(x1, w->L.W); y1 = std::min(y1, w->L.H); z1 = std::min(z1, w->L.W);
+    if (x0 >= x1 || y0 >= y1 || z0 >= z1) return VRT_OK;
+    int st = ensure_depth_table();
+    if (st) return st;
+    uint64_t n = (uint64_t)(x1 - x0) * (y1 - y0) * (z1 - z0);
+    fix_depth_field_kernel<<<blocks_for(n, 256), 256, 0, S(stream)>>>(w->d_words, w->L, x0, y0, z0, x1 - x0,
+                                                                      y1 - y0, z1 - z0, 0, 0, 0, 0);
+    VRT_CUDA(cudaGetLastError());
+    w->has_depth_field = 1;
+    return refresh_masks_box(w, x0, y0, z0, x1, y1, z1, S(stream));
+}
+
+int vrt_remove_sphere(vrt_world* w, int32_t cx, int32_t cy, int32_t cz, int32_t radius, int32_t refresh_depth_field,
+                      void* stream) {
+    if (!w) return set_error(VRT_EINVAL, "NULL world");
+    if (radius < 0 || radius > 1024) return set_error(VRT_ERANGE, "radius %d outside [0, 1024]", radius);
+    if (radius > 0) {
+        uint64_t n = (uint64_t)(2 * radius) * (2 * radius) * (2 * radius);
+        remove_sphere_kernel<<<blocks_for(n, 256), 256, 0, S(stream)>>>(w->d_words, w->L, cx, cy, cz, radius);
+        VRT_CUDA(cudaGetLastError());
+    }
+    int r2 = radius + (7 >> 1);  // DEPTH_FIELD_RADIUS >> 1, level.cpp:43
+    if (refresh_depth_field && r2 > 0) {
+        int st = ensure_depth_table();
+        if (st) return st;
+        int n = 2 * r2;
+        uint64_t cnt = (uint64_t)n * n * n;
+        fix_depth_field_kernel<<<blocks_for(cnt, 256), 256, 0, S(stream)>>>(w->d_words, w->L, cx - r2, cy - r2,
+                                                                            cz - r2, n, n, n, cx, cy, cz, r2);
+        VRT_CUDA(cudaGetLastError());
+        w->has_depth_field = 1;
+    }
+    int rb = std::max(radius, refresh_depth_field ? r2 : radius);
+    return refresh_masks_box(w, cx - rb, cy - rb, cz - rb, cx + rb, cy + rb, cz + rb, S(stream));
+}
+
+int vrt_world_init_reference(vrt_world* w, void* stream) {
+    if (!w) return set_error(VRT_EINVAL, "NULL world");
+    const Layout& L = w->L;
+    // trees at x % 30 == 0 and z % 25 == 0 for x, z in [10, W-10) (level.cpp:130-137)
+    int trees_x = 0, trees_z = 0;
+    for (int x = 10; x < L.W - 10; x++) trees_x += (x % 30 == 0);
+    for (int z = 10; z < L.W - 10; z++) trees_z += (z % 25 == 0);
+    init_reference_layers_kernel<<<blocks_for(L.n_words, 256), 256, 0, S(stream)>>>(w->d_words, L,
+                                                                                    trees_x * trees_z > 0);
+    VRT_CUDA(cudaGetLastError());
+    if (trees_x * trees_z > 0) {
+        dim3 grid(blocks_for(12 * 16 * 12, 256), trees_x * trees_z);
+        init_reference_trees_kernel<<<grid, 256, 0, S(stream)>>>(w->d_words, L, trees_x);
+        VRT_CUDA(cudaGetLastError());
+    }
+    VRT_CUDA(cudaMemsetAsync(w->d_flag, 0, sizeof(int), S(stream)));
+    w->has_depth_field = 0;
+    return refresh_masks_box(w, 0, 0, 0, L.W, L.H, L.W, S(stream));
+}
+
+}  // extern "C"
