@@ -180,9 +180,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true", help="skip the batched / served / CPU legs")
-    ap.add_argument("--kernel", default="mask", choices=["mask", "word"])
+    ap.add_argument("--kernel", default="pixel", choices=["pixel", "mask", "word"])
     ap.add_argument("--tile", default="8x4")
     ap.add_argument("--refill", type=int, default=8)
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
@@ -215,9 +216,10 @@ def main():
     world.upload(sc.words)
     r = vrt.Renderer()
     opts = vrt.RenderOpts()
-    opts.kernel = vrt.KERNEL_BITMASK if args.kernel == "mask" else vrt.KERNEL_WORD
+    opts.kernel = {"pixel": vrt.KERNEL_MASK_PIXEL, "mask": vrt.KERNEL_BITMASK, "word": vrt.KERNEL_WORD}[args.kernel]
     opts.tile_w, opts.tile_h = (int(v) for v in args.tile.split("x"))
     opts.refill_min = args.refill
+    opts.blocks_per_sm = args.blocks_per_sm
     W, H = sc.width, sc.height
     img = torch.empty(W * H * 4, dtype=torch.uint8, device=dev)
     stats = torch.zeros(vrt.STAT_COUNT, dtype=torch.int64, device=dev)
@@ -274,7 +276,7 @@ def main():
     peak, peak_src = measured_peaks()
     algo_bytes = 4 * steps + 4 * hits + 4 * pixels
     achieved = algo_bytes / (ms * 1e-3) / 1e9
-    kname = "render_mask_kernel" if args.kernel == "mask" else "render_word_kernel"
+    kname = {"pixel": "render_mask_pixel_kernel", "mask": "render_mask_kernel", "word": "render_word_kernel"}[args.kernel]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": load_traffic(kname, "full"), "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": algo_bytes, "kernel": kname,

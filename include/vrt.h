@@ -85,18 +85,24 @@ typedef struct vrt_debug_out {
 } vrt_debug_out;
 
 /* Optional device counters accumulated by a render (8 x uint64, device memory,
- * caller zeroes): [0] rays cast, [1] DDA iterations, [2] primary hits, [3] pixels. */
+ * caller zeroes): [0] rays cast, [1] DDA iterations, [2] primary hits, [3] pixels;
+ * traversal diagnostics of the occupancy-mask kernels: [4] box refills (steps that left
+ * a known-empty box or brick), [5] warp slow phases, [6] warp fast batches. */
 #define VRT_STAT_RAYS 0
 #define VRT_STAT_STEPS 1
 #define VRT_STAT_HITS 2
 #define VRT_STAT_PIXELS 3
+#define VRT_STAT_REFILLS 4
+#define VRT_STAT_SLOW 5
+#define VRT_STAT_FAST 6
 #define VRT_STAT_COUNT 8
 
-/* Render kernel choice. AUTO picks the occupancy-mask kernel unless the world holds
- * depth-field words, which only the word kernel follows. */
+/* Render kernel choice. AUTO picks the per-pixel occupancy-mask kernel unless the world
+ * holds depth-field words, which only the word kernel follows. */
 #define VRT_KERNEL_AUTO 0
 #define VRT_KERNEL_WORD 1     /* one thread per pixel, one 4-byte word per DDA step */
 #define VRT_KERNEL_BITMASK 2  /* occupancy-mask traversal, persistent ray refill    */
+#define VRT_KERNEL_MASK_PIXEL 3 /* occupancy-mask traversal, one thread per pixel     */
 
 typedef struct vrt_render_opts {
     int32_t kernel;          /* VRT_KERNEL_*                                        */

@@ -69,7 +69,9 @@ def test_batch_tilings_and_graph(cuda, batch_setup, tile, refill):
     got, gstats = _batch(cuda, r, w, views, opts, graph=True)
     for a, b in zip(base, got):
         assert np.array_equal(a, b)
-    assert np.array_equal(bstats, gstats)
+    # rays, steps, hits and pixels are fixed by the frame; the traversal diagnostics
+    # (refills, slow phases, fast batches) depend on the tiling
+    assert np.array_equal(bstats[:, :4], gstats[:, :4])
 
 
 def test_batch_rejects_mixed_worlds(cuda, batch_setup):

@@ -182,7 +182,7 @@ def kat_scenes():
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("kernel", [vrt.KERNEL_WORD, vrt.KERNEL_BITMASK])
+@pytest.mark.parametrize("kernel", [vrt.KERNEL_WORD, vrt.KERNEL_BITMASK, vrt.KERNEL_MASK_PIXEL])
 def test_kernels_on_known_answer_scenes(cuda, oracle, kernel):
     for name, words, u, width, height in kat_scenes():
         o = oracle.render(words, S, S, u, width, height)

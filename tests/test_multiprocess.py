@@ -1,0 +1,50 @@
+"""The N>1 path (replicas) with two gloo ranks on CPU: the camera shares cover every
+camera exactly once, and whole-job throughput uses the slowest rank's time."""
+import os
+import socket
+
+import pytest
+
+torch = pytest.importorskip("torch")
+import torch.distributed as dist  # noqa: E402
+import torch.multiprocessing as mp  # noqa: E402
+
+
+def _free_port():
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    return port
+
+
+def _worker(rank, world_size, port, out):
+    import sys
+    sys.path.insert(0, os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "voxel-rt_gb300"))
+    import replicas
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world_size)
+    mine = replicas.share(64, rank, world_size)
+    gathered = [None] * world_size
+    dist.all_gather_object(gathered, mine)
+    t = replicas.max_over_ranks(1.0 + rank, dist)
+    rate = replicas.whole_job_rate(len(mine), t, world_size)
+    out[rank] = (gathered, t, rate)
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_replicas():
+    world_size = 2
+    port = _free_port()
+    with mp.Manager() as m:
+        out = m.dict()
+        mp.spawn(_worker, args=(world_size, port, out), nprocs=world_size, join=True)
+        res = dict(out)
+    gathered, t0, rate0 = res[0]
+    _, t1, rate1 = res[1]
+    cams = sorted(c for part in gathered for c in part)
+    assert cams == list(range(64))
+    assert t0 == t1 == 2.0  # the slowest rank's time on every rank
+    assert rate0 == rate1 == 64 / 2.0

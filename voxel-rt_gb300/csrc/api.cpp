@@ -23,6 +23,7 @@ int set_error(int status, const char* fmt, ...) {
 }
 
 int cuda_error(cudaError_t e, const char* what) {
+    cudaGetLastError();  // clear a non-sticky error so later calls do not report it again
     return set_error(VRT_ECUDA, "%s: %s (%d)", what, cudaGetErrorString(e), (int)e);
 }
 

@@ -177,6 +177,8 @@ struct ViewDev {
     int width, height;
     int tiles_x;
     int tile_begin;  // first global tile of this view
+    int tile_w, tile_h;
+    int refill_min;  // lanes parked before a warp runs its slow phase (tile's view decides)
     uint8_t* rgba;
     vrt_debug_out dbg;
     unsigned long long* stats;
@@ -185,96 +187,49 @@ struct ViewDev {
 struct MaskParams {
     const int32_t* words;
     const uint64_t* bricks;
-    const uint64_t* regions;
-    const uint64_t* supers;
+    const uint8_t* bdist;
+    const uint8_t* rdist;
     Layout L;
     const ViewDev* views;  // nviews entries (device); NULL when nviews == 1 (v0 is used)
     int nviews;
     int total_tiles;
-    int tile_w, tile_h;
-    int refill_min;
+    int region_bytes16;    // region distance bytes rounded up to 16 (staged in shared memory when small)
     unsigned int* tile_counter;
     ViewDev v0;
 };
 
+enum { M_RUN = 0, M_BOX = 1, M_HIT = 2, M_MISS = 3, M_IDLE = 4, M_DONE = 5 };
+enum { PH_PRIMARY = 0, PH_GLOBAL = 1, PH_LOCAL0 = 2 };
 enum { T_LIVE = 0, T_HIT = 1, T_MISS = 2 };
-enum { PH_IDLE = -1, PH_PRIMARY = 0, PH_GLOBAL = 1, PH_LOCAL0 = 2 };
 
-struct Trav {
+// Per-lane pixel state kept in shared memory (structure of arrays, 256 lanes): it is
+// touched only between rays, so the traversal loop keeps only the ray in registers.
+enum {
+    F_PIX, F_VID, F_HPX, F_HPY, F_HPZ, F_MR, F_MG, F_MB, F_HIT, F_CAST, F_OCC, F_STEPS, F_PSTEPS, F_HN,
+    F_ST_VID, F_ST_RAYS, F_ST_HITS, F_ST_PIX, F_ST_STEPS_LO, F_ST_STEPS_HI, F_ST_REFILLS, NF
+};
+constexpr int kThreads = 256;
+constexpr int kUnroll = 4;
+
+__device__ __forceinline__ const ViewDev& view_of(const MaskParams& P, int v) {
+    return P.nviews == 1 ? P.v0 : P.views[v];
+}
+
+struct Ray {
     int cx, cy, cz;
     int sx, sy, sz;
+    int ex, ey, ez;  // cell coordinate at which the ray leaves its known box, per axis
+    int rem;         // DDA iterations left
+    int la;          // axis of the parked step
     float tx, ty, tz;
     float dx, dy, dz;
-    int rem;         // DDA iterations left
-    int ex, ey, ez;  // cell coordinate at which the ray leaves the current box, per axis
-    uint64_t m;      // voxel bits of the current brick (0 for an empty box)
-    float cd;        // currDist of the last step
-    int la;          // axis of the last step
+    uint64_t m;      // voxel bits of the current brick (0 inside an empty box)
 };
 
-// The ray just entered cell c outside its known box: find the largest empty node of
-// the hierarchy holding c (super block, region or brick), or load the brick's bits.
-__device__ __forceinline__ int refill(Trav& r, const MaskParams& P) {
-    const Layout& L = P.L;
-    if ((unsigned)r.cx >= (unsigned)L.W || (unsigned)r.cy >= (unsigned)L.H || (unsigned)r.cz >= (unsigned)L.W)
-        return T_MISS;  // left the world: getVoxelIndex == -1
-    const uint64_t sidx = (uint64_t)(r.cx >> 6) + (uint64_t)L.SW * ((uint64_t)(r.cy >> 6) + (uint64_t)L.SH * (r.cz >> 6));
-    const uint64_t sm = __ldg(P.supers + sidx);
-    int shift;
-    uint64_t m = 0;
-    if (sm == 0) {
-        shift = 6;
-    } else {
-        const int rb = ((r.cx >> 4) & 3) + 4 * ((r.cy >> 4) & 3) + 16 * ((r.cz >> 4) & 3);
-        if (!((sm >> rb) & 1)) {
-            shift = 4;
-        } else {
-            const uint64_t ridx = sidx * 64 + rb;
-            const uint64_t rm = __ldg(P.regions + ridx);
-            const int bb = ((r.cx >> 2) & 3) + 4 * ((r.cy >> 2) & 3) + 16 * ((r.cz >> 2) & 3);
-            shift = 2;
-            if ((rm >> bb) & 1) m = __ldg(P.bricks + ridx * 64 + bb);
-        }
-    }
-    const int lox = (r.cx >> shift) << shift, loy = (r.cy >> shift) << shift, loz = (r.cz >> shift) << shift;
-    const int size = 1 << shift;
-    const int hix = min(lox + size, L.W), hiy = min(loy + size, L.H), hiz = min(loz + size, L.W);
-    r.ex = r.sx > 0 ? hix : (r.sx < 0 ? lox - 1 : INT_MIN);
-    r.ey = r.sy > 0 ? hiy : (r.sy < 0 ? loy - 1 : INT_MIN);
-    r.ez = r.sz > 0 ? hiz : (r.sz < 0 ? loz - 1 : INT_MIN);
-    r.m = m;
-    if (m) {
-        const int bit = (r.cx & 3) + 4 * (r.cy & 3) + 16 * (r.cz & 3);
-        if ((m >> bit) & 1) return T_HIT;
-    }
-    return T_LIVE;
-}
-
-// One iteration of castRay's loop (fshader.glsl:83-126).
-__device__ __forceinline__ int dda_step(Trav& r, const MaskParams& P) {
-    if (r.rem == 0) return T_MISS;
-    r.rem--;
-    const bool bx = r.tx < r.ty && r.tx < r.tz;
-    const bool by = !bx && r.ty < r.tx && r.ty < r.tz;
-    bool out;
-    if (bx) {
-        r.cd = r.tx; r.tx = fadd(r.tx, r.dx); r.cx += r.sx; out = r.cx == r.ex; r.la = 0;
-    } else if (by) {
-        r.cd = r.ty; r.ty = fadd(r.ty, r.dy); r.cy += r.sy; out = r.cy == r.ey; r.la = 1;
-    } else {
-        r.cd = r.tz; r.tz = fadd(r.tz, r.dz); r.cz += r.sz; out = r.cz == r.ez; r.la = 2;
-    }
-    if (out) return refill(r, P);
-    if (r.m) {
-        const int bit = (r.cx & 3) + 4 * (r.cy & 3) + 16 * (r.cz & 3);
-        if ((r.m >> bit) & 1) return T_HIT;
-    }
-    return T_LIVE;
-}
-
-// Start a ray at o along d with loop bound n; the first step always refills, because
-// the known box is empty (each exit coordinate is the first cell the step reaches).
-__device__ __forceinline__ void start_ray(Trav& r, V3 o, V3 d, int n, int maxSteps) {
+// Start a ray at o along d with loop bound n (fshader.glsl:64-79).  The known box is
+// empty: every exit coordinate is the first cell a step along that axis reaches, so the
+// first step always parks the lane for a refill.
+__device__ __forceinline__ int start_ray(Ray& r, V3 o, V3 d, int n, int maxSteps) {
     RaySetup s;
     ray_setup(o, d, s);
     r.cx = s.cx; r.cy = s.cy; r.cz = s.cz;
@@ -284,66 +239,120 @@ __device__ __forceinline__ void start_ray(Trav& r, V3 o, V3 d, int n, int maxSte
     r.rem = max(0, min(n, maxSteps));
     r.ex = s.cx + s.sx; r.ey = s.cy + s.sy; r.ez = s.cz + s.sz;
     r.m = 0;
-    r.cd = 0.0f;
     r.la = 2;
+    return r.rem;
 }
 
-__device__ __forceinline__ const ViewDev& view_of(const MaskParams& P, int v) {
-    return P.nviews == 1 ? P.v0 : P.views[v];
+// The parked step moved the ray into cell c outside its box: bound the largest known
+// box around c from the distance fields, or load the brick's voxel bits.
+template <bool SMEM>
+__device__ __forceinline__ int refill(Ray& r, const MaskParams& P, const uint8_t* rdist) {
+    const Layout& L = P.L;
+    if ((unsigned)r.cx >= (unsigned)L.W || (unsigned)r.cy >= (unsigned)L.H || (unsigned)r.cz >= (unsigned)L.W)
+        return T_MISS;  // getVoxelIndex == -1 (fshader.glsl:123-125)
+    const int rx = r.cx >> 4, ry = r.cy >> 4, rz = r.cz >> 4;
+    const uint64_t rl = region_linear(L, rx, ry, rz);
+    const int dr = SMEM ? (int)rdist[rl] : (int)__ldg(rdist + rl);
+    int lox, loy, loz, hix, hiy, hiz;
+    uint64_t m = 0;
+    if (dr > 0) {  // every region within Chebyshev radius dr-1 is empty
+        const int k = dr - 1;
+        lox = (rx - k) << 4; loy = (ry - k) << 4; loz = (rz - k) << 4;
+        hix = (rx + k + 1) << 4; hiy = (ry + k + 1) << 4; hiz = (rz + k + 1) << 4;
+    } else {
+        const int bx = r.cx >> 2, by = r.cy >> 2, bz = r.cz >> 2;
+        const uint64_t bi = brick_index(L, bx, by, bz);
+        m = __ldg(P.bricks + bi);
+        const int db = __ldg(P.bdist + bi);
+        const int k = m ? 0 : max(db, 1) - 1;
+        lox = (bx - k) << 2; loy = (by - k) << 2; loz = (bz - k) << 2;
+        hix = (bx + k + 1) << 2; hiy = (by + k + 1) << 2; hiz = (bz + k + 1) << 2;
+    }
+    lox = max(lox, 0); loy = max(loy, 0); loz = max(loz, 0);
+    hix = min(hix, L.W); hiy = min(hiy, L.H); hiz = min(hiz, L.W);
+    r.ex = r.sx > 0 ? hix : (r.sx < 0 ? lox - 1 : INT_MIN);
+    r.ey = r.sy > 0 ? hiy : (r.sy < 0 ? loy - 1 : INT_MIN);
+    r.ez = r.sz > 0 ? hiz : (r.sz < 0 ? loz - 1 : INT_MIN);
+    r.m = m;
+    const int bit = (r.cx & 3) | ((r.cy & 3) << 2) | ((r.cz & 3) << 4);
+    return ((m >> bit) & 1) ? T_HIT : T_LIVE;
 }
 
-__global__ void __launch_bounds__(256, 3) render_mask_kernel(const __grid_constant__ MaskParams P) {
+template <bool SMEM, int MINB>
+__global__ void __launch_bounds__(kThreads, MINB) render_mask_kernel(const __grid_constant__ MaskParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const uint8_t* rdist = P.rdist;
+    uint32_t* ls = reinterpret_cast<uint32_t*>(smem);
+    if (SMEM) {
+        const uint4* src = reinterpret_cast<const uint4*>(P.rdist);
+        uint4* dst = reinterpret_cast<uint4*>(smem);
+        for (int i = threadIdx.x; i < P.region_bytes16 / 16; i += kThreads) dst[i] = __ldg(src + i);
+        rdist = smem;
+        ls = reinterpret_cast<uint32_t*>(smem + P.region_bytes16);
+    }
+#define LSU(f) ls[(f) * kThreads + threadIdx.x]
+#define LSF(f) reinterpret_cast<float*>(ls)[(f) * kThreads + threadIdx.x]
+    LSU(F_ST_VID) = 0xffffffffu;
+    LSU(F_ST_RAYS) = 0; LSU(F_ST_HITS) = 0; LSU(F_ST_PIX) = 0; LSU(F_ST_STEPS_LO) = 0; LSU(F_ST_STEPS_HI) = 0;
+    LSU(F_ST_REFILLS) = 0;
+    if (SMEM) __syncthreads();
+    unsigned n_slow = 0, n_fast = 0;  // warp-uniform diagnostics
+
     const int lane = threadIdx.x & 31;
     const unsigned lt = (1u << lane) - 1u;
     const unsigned FULL = 0xffffffffu;
-    const int tile_px = P.tile_w * P.tile_h;
 
     // warp tile queue (uniform across the warp)
-    int q_pos = 0, q_size = 0, q_vid = 0, q_x0 = 0, q_y0 = 0, q_w = 0, q_h = 0;
+    int q_pos = 0, q_size = 0, q_vid = 0, q_x0 = 0, q_y0 = 0, q_w = 0, q_h = 0, q_tw = 1, q_thr = 8;
     bool q_empty = false;
 
-    // lane state
-    int phase = PH_IDLE;
-    int vid = 0, pix = 0;
-    float hpx = 0.f, hpy = 0.f, hpz = 0.f;
-    int hn_axis = 2, hn_s = 0;
-    float mr = 0.f, mg = 0.f, mb = 0.f;
-    int32_t hit = -1;
-    uint32_t cast = 0, occ = 0;
-    int steps = 0, psteps = 0;
-    bool live = false;
-    int status = T_MISS;
-    Trav r;
-    r.rem = 0; r.m = 0;
+    int mode = M_IDLE, phase = PH_PRIMARY;
+    Ray r;
+    r.cx = r.cy = r.cz = 0; r.sx = r.sy = r.sz = 0; r.ex = r.ey = r.ez = 0; r.rem = 0; r.la = 2;
+    r.tx = r.ty = r.tz = 0.f; r.dx = r.dy = r.dz = 0.f; r.m = 0;
 
-    // per-lane counters, flushed when the lane moves to another view and at exit
-    int st_vid = -1;
-    unsigned long long st_steps = 0;
-    unsigned st_rays = 0, st_hits = 0, st_pix = 0;
-
-    while (true) {
-        // ---- 1. lanes whose ray ended: fold the result in and pick the pixel's next ray
+    for (;;) {
+        // ================= slow phase =================
+        // (a) parked box exits: refill from the hierarchy, finish the parked step
+        n_slow++;
+        if (mode == M_BOX) {
+            LSU(F_ST_REFILLS) += 1u;
+            const int t = refill<SMEM>(r, P, rdist);
+            if (t == T_LIVE) {
+                if (r.la == 0) r.tx = fadd(r.tx, r.dx);
+                else if (r.la == 1) r.ty = fadd(r.ty, r.dy);
+                else r.tz = fadd(r.tz, r.dz);
+                mode = r.rem == 0 ? M_MISS : M_RUN;
+            } else {
+                mode = t == T_HIT ? M_HIT : M_MISS;
+            }
+        }
+        // (b) ended rays: fold the result into the pixel, pick the pixel's next ray
         bool want = false;
         V3 o{0.f, 0.f, 0.f}, d{0.f, 0.f, 0.f};
         int n = 0;
-        if (phase != PH_IDLE && !live) {
+        if (mode == M_HIT || mode == M_MISS) {
+            const int vid = (int)LSU(F_VID), pix = (int)LSU(F_PIX);
             const ViewDev& V = view_of(P, vid);
             const vrt_uniforms& u = V.u;
-            steps -= r.rem;  // iterations this ray did not use
+            int steps = (int)LSU(F_STEPS) - r.rem;  // iterations this ray did not use
+            float mr = LSF(F_MR), mg = LSF(F_MG), mb = LSF(F_MB);
+            int32_t hit = (int32_t)LSU(F_HIT);
+            uint32_t cast = LSU(F_CAST), occ = LSU(F_OCC);
+            int psteps = (int)LSU(F_PSTEPS);
+            V3 hp{LSF(F_HPX), LSF(F_HPY), LSF(F_HPZ)};
             bool done = false;
-            V3 hp{hpx, hpy, hpz};
-            int next = 16;
+            int next = VRT_MAX_LOCAL_LIGHTS;
             if (phase == PH_PRIMARY) {
                 psteps = steps;
-                if (status == T_HIT) {
+                if (mode == M_HIT) {
+                    const float cd = r.la == 0 ? r.tx : (r.la == 1 ? r.ty : r.tz);
                     hit = r.cx + P.L.W * r.cy + P.L.W * P.L.H * r.cz;
                     const int px = pix % V.width, py = pix / V.width;
                     V3 rd = primary_dir(u, px, py, V.width, V.height);
-                    V3 cam{u.camPos[0], u.camPos[1], u.camPos[2]};
-                    hp = add3(mul3s(rd, r.cd), cam);
-                    hpx = hp.x; hpy = hp.y; hpz = hp.z;
-                    hn_axis = r.la;
-                    hn_s = r.la == 0 ? r.sx : (r.la == 1 ? r.sy : r.sz);
+                    hp = add3(mul3s(rd, cd), V3{u.camPos[0], u.camPos[1], u.camPos[2]});
+                    const int s = r.la == 0 ? r.sx : (r.la == 1 ? r.sy : r.sz);
+                    LSU(F_HN) = (uint32_t)(r.la | ((s + 1) << 2));
                 }
                 if (u.viewDepthField == 1) {
                     mr = mg = mb = fdiv((float)psteps, 100.0f);
@@ -351,8 +360,7 @@ __global__ void __launch_bounds__(256, 3) render_mask_kernel(const __grid_consta
                 } else if (hit < 0) {
                     done = true;
                 } else {
-                    V3 lp{u.lightPos[0], u.lightPos[1], u.lightPos[2]};
-                    V3 toLight = norm3(sub3(lp, hp));
+                    V3 toLight = norm3(sub3(V3{u.lightPos[0], u.lightPos[1], u.lightPos[2]}, hp));
                     o = add3(hp, mul3s(toLight, 0.001f));
                     d = toLight;
                     n = u.maxSteps;
@@ -360,37 +368,37 @@ __global__ void __launch_bounds__(256, 3) render_mask_kernel(const __grid_consta
                     phase = PH_GLOBAL;
                 }
             } else {
-                V3 hn = axis_normal(hn_axis, hn_s);
+                const uint32_t hn_code = LSU(F_HN);
+                const V3 hn = axis_normal((int)(hn_code & 3), (int)(hn_code >> 2) - 1);
                 if (phase == PH_GLOBAL) {
                     cast |= 1u;
-                    if (status == T_HIT) {
+                    if (mode == M_HIT) {
                         occ |= 1u;
                     } else {
-                        V3 lp{u.lightPos[0], u.lightPos[1], u.lightPos[2]};
-                        V3 toLight = norm3(sub3(lp, hp));
-                        float c = fmul(u.diffuse, fmax0(dot3(hn, toLight)));
+                        V3 toLight = norm3(sub3(V3{u.lightPos[0], u.lightPos[1], u.lightPos[2]}, hp));
+                        const float c = fmul(u.diffuse, fmax0(dot3(hn, toLight)));
                         mr = fadd(mr, c); mg = fadd(mg, c); mb = fadd(mb, c);
                     }
                     next = 0;
                 } else {
                     const int i = phase - PH_LOCAL0;
                     cast |= 2u << i;
-                    if (status == T_HIT) {
+                    if (mode == M_HIT) {
                         occ |= 2u << i;
                     } else {
-                        V3 Lp{u.localLights[i][0], u.localLights[i][1], u.localLights[i][2]};
-                        float ld = len3(sub3(Lp, hp));
-                        V3 tl = norm3(sub3(Lp, hp));
-                        float nl = fmax0(dot3(hn, tl));
-                        float fall = fdiv(fsub(u.localLightDist, ld), u.localLightDist);
-                        float a = u.localLights[i][3];
+                        const V3 Lp{u.localLights[i][0], u.localLights[i][1], u.localLights[i][2]};
+                        const float ld = len3(sub3(Lp, hp));
+                        const V3 tl = norm3(sub3(Lp, hp));
+                        const float nl = fmax0(dot3(hn, tl));
+                        const float fall = fdiv(fsub(u.localLightDist, ld), u.localLightDist);
+                        const float a = u.localLights[i][3];
                         mr = fadd(mr, fmul(fmul(fmul(a, u.localLightColor[i][0]), nl), fall));
                         mg = fadd(mg, fmul(fmul(fmul(a, u.localLightColor[i][1]), nl), fall));
                         mb = fadd(mb, fmul(fmul(fmul(a, u.localLightColor[i][2]), nl), fall));
                     }
                     next = i + 1;
                 }
-                // fshader.glsl:159-181: overbright test before each light, then range test
+                // fshader.glsl:159-181: overbright test before each light, then the range test
                 const float ob = u.maxOverbright;
                 for (int i = next; i < VRT_MAX_LOCAL_LIGHTS; i++) {
                     if (mr >= ob && mg >= ob && mb >= ob) {
@@ -398,10 +406,10 @@ __global__ void __launch_bounds__(256, 3) render_mask_kernel(const __grid_consta
                         break;
                     }
                     if (u.localLights[i][0] >= 0 && u.localLights[i][1] >= 0 && u.localLights[i][2] >= 0) {
-                        V3 Lp{u.localLights[i][0], u.localLights[i][1], u.localLights[i][2]};
-                        float ld = len3(sub3(Lp, hp));
+                        const V3 Lp{u.localLights[i][0], u.localLights[i][1], u.localLights[i][2]};
+                        const float ld = len3(sub3(Lp, hp));
                         if (ld <= u.localLightDist) {
-                            V3 tl = norm3(sub3(Lp, hp));
+                            const V3 tl = norm3(sub3(Lp, hp));
                             o = add3(hp, mul3s(tl, 0.001f));
                             d = tl;
                             n = f2i(fadd(ld, 1.0f));
@@ -414,7 +422,7 @@ __global__ void __launch_bounds__(256, 3) render_mask_kernel(const __grid_consta
                 done = !want;
             }
             if (done) {
-                int32_t word = hit >= 0 ? __ldg(P.words + hit) : 0;
+                const int32_t word = hit >= 0 ? __ldg(P.words + hit) : 0;
                 PixelResult res;
                 res.rgba = pack_color(u, hit >= 0, word, mr, mg, mb, psteps);
                 res.hit = hit; res.cast = cast; res.occ = occ;
@@ -422,27 +430,39 @@ __global__ void __launch_bounds__(256, 3) render_mask_kernel(const __grid_consta
                 res.mr = mr; res.mg = mg; res.mb = mb;
                 store_pixel(V.dbg, V.rgba, (uint64_t)pix, res);
                 if (V.stats) {
-                    if (st_vid != vid) {
-                        if (st_vid >= 0) {
-                            unsigned long long* s = view_of(P, st_vid).stats;
-                            atomicAdd(s + VRT_STAT_RAYS, (unsigned long long)st_rays);
-                            atomicAdd(s + VRT_STAT_STEPS, st_steps);
-                            atomicAdd(s + VRT_STAT_HITS, (unsigned long long)st_hits);
-                            atomicAdd(s + VRT_STAT_PIXELS, (unsigned long long)st_pix);
+                    if (LSU(F_ST_VID) != (uint32_t)vid) {
+                        if (LSU(F_ST_VID) != 0xffffffffu) {  // the lane moves to another view: flush
+                            unsigned long long* s = view_of(P, (int)LSU(F_ST_VID)).stats;
+                            atomicAdd(s + VRT_STAT_RAYS, (unsigned long long)LSU(F_ST_RAYS));
+                            atomicAdd(s + VRT_STAT_STEPS, ((unsigned long long)LSU(F_ST_STEPS_HI) << 32) | LSU(F_ST_STEPS_LO));
+                            atomicAdd(s + VRT_STAT_HITS, (unsigned long long)LSU(F_ST_HITS));
+                            atomicAdd(s + VRT_STAT_PIXELS, (unsigned long long)LSU(F_ST_PIX));
+                            atomicAdd(s + VRT_STAT_REFILLS, (unsigned long long)LSU(F_ST_REFILLS));
+                            LSU(F_ST_RAYS) = 0; LSU(F_ST_HITS) = 0; LSU(F_ST_PIX) = 0;
+                            LSU(F_ST_STEPS_LO) = 0; LSU(F_ST_STEPS_HI) = 0; LSU(F_ST_REFILLS) = 0;
                         }
-                        st_vid = vid; st_rays = 0; st_steps = 0; st_hits = 0; st_pix = 0;
+                        LSU(F_ST_VID) = (uint32_t)vid;
                     }
-                    st_rays += 1u + __popc(cast);
-                    st_steps += (unsigned)steps;
-                    st_hits += hit >= 0;
-                    st_pix += 1;
+                    LSU(F_ST_RAYS) += 1u + __popc(cast);
+                    const unsigned long long s64 =
+                        (((unsigned long long)LSU(F_ST_STEPS_HI) << 32) | LSU(F_ST_STEPS_LO)) + (unsigned)steps;
+                    LSU(F_ST_STEPS_LO) = (uint32_t)s64;
+                    LSU(F_ST_STEPS_HI) = (uint32_t)(s64 >> 32);
+                    LSU(F_ST_HITS) += hit >= 0;
+                    LSU(F_ST_PIX) += 1u;
                 }
-                phase = PH_IDLE;
+                mode = M_IDLE;
+            } else {
+                LSF(F_MR) = mr; LSF(F_MG) = mg; LSF(F_MB) = mb;
+                LSU(F_HIT) = (uint32_t)hit; LSU(F_CAST) = cast; LSU(F_OCC) = occ;
+                LSU(F_PSTEPS) = (uint32_t)psteps;
+                LSF(F_HPX) = hp.x; LSF(F_HPY) = hp.y; LSF(F_HPZ) = hp.z;
             }
+            LSU(F_STEPS) = (uint32_t)steps;
         }
 
-        // ---- 2. hand new pixels to idle lanes from the warp's tile queue
-        unsigned need = __ballot_sync(FULL, phase == PH_IDLE);
+        // (c) hand new pixels to idle lanes from the warp's tile queue
+        unsigned need = __ballot_sync(FULL, mode == M_IDLE);
         while (need && !q_empty) {
             if (q_pos >= q_size) {
                 unsigned t = 0;
@@ -459,70 +479,245 @@ __global__ void __launch_bounds__(256, 3) render_mask_kernel(const __grid_consta
                 const ViewDev& V = view_of(P, v);
                 const int lt_idx = (int)t - V.tile_begin;
                 q_vid = v;
-                q_x0 = (lt_idx % V.tiles_x) * P.tile_w;
-                q_y0 = (lt_idx / V.tiles_x) * P.tile_h;
+                q_tw = V.tile_w;
+                q_x0 = (lt_idx % V.tiles_x) * V.tile_w;
+                q_y0 = (lt_idx / V.tiles_x) * V.tile_h;
                 q_w = V.width;
                 q_h = V.height;
+                q_thr = V.refill_min;
                 q_pos = 0;
-                q_size = tile_px;
+                q_size = V.tile_w * V.tile_h;
             }
             const int rank = __popc(need & lt);
             const int take = min(__popc(need), q_size - q_pos);
             if (((need >> lane) & 1) && rank < take) {
                 const int pos = q_pos + rank;
-                const int px = q_x0 + pos % P.tile_w, py = q_y0 + pos / P.tile_w;
+                const int px = q_x0 + pos % q_tw, py = q_y0 + pos / q_tw;
                 if (px < q_w && py < q_h) {
                     const vrt_uniforms& u = view_of(P, q_vid).u;
-                    vid = q_vid;
-                    pix = py * q_w + px;
-                    phase = PH_PRIMARY;
-                    hit = -1; cast = 0; occ = 0; steps = 0; psteps = 0;
-                    mr = mg = mb = u.ambient;
-                    hpx = hpy = hpz = 0.0f;
-                    hn_axis = 2; hn_s = 0;
+                    LSU(F_VID) = (uint32_t)q_vid;
+                    LSU(F_PIX) = (uint32_t)(py * q_w + px);
+                    LSU(F_HIT) = 0xffffffffu;
+                    LSU(F_CAST) = 0; LSU(F_OCC) = 0; LSU(F_STEPS) = 0; LSU(F_PSTEPS) = 0;
+                    LSF(F_MR) = u.ambient; LSF(F_MG) = u.ambient; LSF(F_MB) = u.ambient;
+                    LSF(F_HPX) = 0.f; LSF(F_HPY) = 0.f; LSF(F_HPZ) = 0.f;
+                    LSU(F_HN) = 2u | (1u << 2);
                     o = V3{u.camPos[0], u.camPos[1], u.camPos[2]};
                     d = primary_dir(u, px, py, q_w, q_h);
                     n = u.maxSteps;
                     want = true;
+                    phase = PH_PRIMARY;
+                    mode = M_RUN;
                 }
             }
             q_pos += take;
-            need = __ballot_sync(FULL, phase == PH_IDLE);
+            need = __ballot_sync(FULL, mode == M_IDLE);
         }
+        if (mode == M_IDLE && q_empty) mode = M_DONE;
 
-        // ---- 3. set up the new rays together
+        // (d) set up the new rays together
         if (want) {
-            const int maxSteps = view_of(P, vid).u.maxSteps;
-            start_ray(r, o, d, n, maxSteps);
-            steps += r.rem;
-            live = true;
+            const int vid = (int)LSU(F_VID);
+            const int rem = start_ray(r, o, d, n, view_of(P, vid).u.maxSteps);
+            LSU(F_STEPS) += (uint32_t)rem;
+            mode = rem == 0 ? M_MISS : M_RUN;
         }
 
-        const unsigned act = __ballot_sync(FULL, phase != PH_IDLE);
+        const unsigned act = __ballot_sync(FULL, mode != M_DONE);
         if (act == 0) break;
 
-        // ---- 4. traverse until enough lanes need a refill
-        const int thr = min(P.refill_min, __popc(act));
-        while (true) {
-            if (live) {
-                int st = dda_step(r, P);
-                if (st != T_LIVE) { live = false; status = st; }
+        // ================= fast phase: DDA steps in registers =================
+        const int thr = min(q_thr, __popc(act));
+        for (;;) {
+            n_fast++;
+#pragma unroll
+            for (int k = 0; k < kUnroll; k++) {
+                if (mode == M_RUN) {
+                    // one iteration of castRay's loop (fshader.glsl:83-126) inside a known box
+                    const bool bx = (r.tx < r.ty) & (r.tx < r.tz);
+                    const bool by = (!bx) & (r.ty < r.tx) & (r.ty < r.tz);
+                    const bool bz = !(bx | by);
+                    if (bx) r.cx += r.sx;
+                    if (by) r.cy += r.sy;
+                    if (bz) r.cz += r.sz;
+                    r.rem -= 1;
+                    const bool out = (r.cx == r.ex) | (r.cy == r.ey) | (r.cz == r.ez);
+                    const int bit = (r.cx & 3) | ((r.cy & 3) << 2) | ((r.cz & 3) << 4);
+                    const bool hb = (r.m >> bit) & 1;
+                    if (out | hb | (r.rem == 0)) {
+                        r.la = bx ? 0 : (by ? 1 : 2);
+                        mode = out ? M_BOX : (hb ? M_HIT : M_MISS);
+                    } else {
+                        if (bx) r.tx = fadd(r.tx, r.dx);
+                        if (by) r.ty = fadd(r.ty, r.dy);
+                        if (bz) r.tz = fadd(r.tz, r.dz);
+                    }
+                }
             }
-            if (live) {
-                int st = dda_step(r, P);
-                if (st != T_LIVE) { live = false; status = st; }
-            }
-            const unsigned fin = __ballot_sync(FULL, phase != PH_IDLE && !live);
-            if (__popc(fin) >= thr) break;
+            const unsigned parked = __ballot_sync(FULL, mode != M_RUN && mode != M_DONE);
+            if (__popc(parked) >= thr) break;
         }
     }
 
-    if (st_vid >= 0) {
-        unsigned long long* s = view_of(P, st_vid).stats;
-        atomicAdd(s + VRT_STAT_RAYS, (unsigned long long)st_rays);
-        atomicAdd(s + VRT_STAT_STEPS, st_steps);
-        atomicAdd(s + VRT_STAT_HITS, (unsigned long long)st_hits);
-        atomicAdd(s + VRT_STAT_PIXELS, (unsigned long long)st_pix);
+    if (LSU(F_ST_VID) != 0xffffffffu) {
+        unsigned long long* s = view_of(P, (int)LSU(F_ST_VID)).stats;
+        atomicAdd(s + VRT_STAT_RAYS, (unsigned long long)LSU(F_ST_RAYS));
+        atomicAdd(s + VRT_STAT_STEPS, ((unsigned long long)LSU(F_ST_STEPS_HI) << 32) | LSU(F_ST_STEPS_LO));
+        atomicAdd(s + VRT_STAT_HITS, (unsigned long long)LSU(F_ST_HITS));
+        atomicAdd(s + VRT_STAT_PIXELS, (unsigned long long)LSU(F_ST_PIX));
+        atomicAdd(s + VRT_STAT_REFILLS, (unsigned long long)LSU(F_ST_REFILLS));
+    }
+    if (lane == 0 && view_of(P, q_vid).stats) {
+        atomicAdd(view_of(P, q_vid).stats + VRT_STAT_SLOW, (unsigned long long)n_slow);
+        atomicAdd(view_of(P, q_vid).stats + VRT_STAT_FAST, (unsigned long long)n_fast);
+    }
+#undef LSU
+#undef LSF
+}
+
+// ---------------------------------------------------------------- mask kernel, one thread per pixel
+
+// castRay (fshader.glsl:59-129) over the occupancy hierarchy: the same per-cell adds and
+// decisions as the shader, memory read only when the ray leaves its known box.
+template <bool SMEM>
+__device__ __forceinline__ int cast_mask(const MaskParams& P, const uint8_t* rdist, V3 o, V3 d, int n, int maxSteps,
+                                         float& cd, int& axis, int& sgn, int& steps, int32_t& hit_index,
+                                         unsigned& refills) {
+    Ray r;
+    const int n0 = start_ray(r, o, d, n, maxSteps);
+    int result = T_MISS;
+    while (r.rem != 0) {
+        r.rem -= 1;
+        const bool bx = (r.tx < r.ty) & (r.tx < r.tz);
+        const bool by = (!bx) & (r.ty < r.tx) & (r.ty < r.tz);
+        const bool bz = !(bx | by);
+        if (bx) r.cx += r.sx;
+        if (by) r.cy += r.sy;
+        if (bz) r.cz += r.sz;
+        const bool out = (r.cx == r.ex) | (r.cy == r.ey) | (r.cz == r.ez);
+        int t = T_LIVE;
+        if (out) {
+            refills++;
+            t = refill<SMEM>(r, P, rdist);
+        } else {
+            const int bit = (r.cx & 3) | ((r.cy & 3) << 2) | ((r.cz & 3) << 4);
+            if ((r.m >> bit) & 1) t = T_HIT;
+        }
+        if (t != T_LIVE) {
+            result = t;
+            axis = bx ? 0 : (by ? 1 : 2);
+            cd = bx ? r.tx : (by ? r.ty : r.tz);
+            sgn = bx ? r.sx : (by ? r.sy : r.sz);
+            break;
+        }
+        if (bx) r.tx = fadd(r.tx, r.dx);
+        if (by) r.ty = fadd(r.ty, r.dy);
+        if (bz) r.tz = fadd(r.tz, r.dz);
+    }
+    steps += n0 - r.rem;
+    if (result == T_HIT) hit_index = r.cx + P.L.W * r.cy + P.L.W * P.L.H * r.cz;
+    return result;
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(128) render_mask_pixel_kernel(const __grid_constant__ MaskParams P) {
+    extern __shared__ __align__(16) uint8_t smem[];
+    const uint8_t* rdist = P.rdist;
+    if (SMEM) {
+        const uint4* src = reinterpret_cast<const uint4*>(P.rdist);
+        uint4* dst = reinterpret_cast<uint4*>(smem);
+        for (int i = threadIdx.x; i < P.region_bytes16 / 16; i += blockDim.x) dst[i] = __ldg(src + i);
+        __syncthreads();
+        rdist = smem;
+    }
+    const ViewDev& V = P.v0;
+    const int px = blockIdx.x * 16 + (threadIdx.x & 15);
+    const int py = blockIdx.y * 8 + (threadIdx.x >> 4);
+    const bool valid = px < V.width && py < V.height;
+    PixelResult res{};
+    unsigned refills = 0;
+    if (valid) {
+        const vrt_uniforms& u = V.u;
+        const V3 cam{u.camPos[0], u.camPos[1], u.camPos[2]};
+        const V3 rd = primary_dir(u, px, py, V.width, V.height);
+        float cd = 0.f;
+        int axis = 2, sgn = 0, steps = 0;
+        int32_t hit = -1, dummy = -1;
+        const int pr = cast_mask<SMEM>(P, rdist, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit, refills);
+        res.primary_steps = steps;
+        float mr = u.ambient, mg = u.ambient, mb = u.ambient;
+        int32_t word = 0;
+        if (u.viewDepthField == 1) {
+            mr = mg = mb = fdiv((float)steps, 100.0f);
+        } else if (pr == T_HIT) {
+            const V3 hp = add3(mul3s(rd, cd), cam);
+            const V3 hn = axis_normal(axis, sgn);
+            const V3 toLight = norm3(sub3(V3{u.lightPos[0], u.lightPos[1], u.lightPos[2]}, hp));
+            float c2;
+            int a2, s2;
+            const int sr = cast_mask<SMEM>(P, rdist, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
+                                           u.maxSteps, c2, a2, s2, steps, dummy, refills);
+            res.cast |= 1u;
+            if (sr != T_HIT) {
+                const float c = fmul(u.diffuse, fmax0(dot3(hn, toLight)));
+                mr = fadd(mr, c); mg = fadd(mg, c); mb = fadd(mb, c);
+            } else {
+                res.occ |= 1u;
+            }
+            const float ob = u.maxOverbright, R = u.localLightDist;
+            for (int i = 0; i < VRT_MAX_LOCAL_LIGHTS; i++) {
+                if (mr >= ob && mg >= ob && mb >= ob) {
+                    mr = mg = mb = ob;
+                    break;
+                } else if (u.localLights[i][0] >= 0 && u.localLights[i][1] >= 0 && u.localLights[i][2] >= 0) {
+                    const V3 Lp{u.localLights[i][0], u.localLights[i][1], u.localLights[i][2]};
+                    const float ld = len3(sub3(Lp, hp));
+                    if (ld <= R) {
+                        const V3 tl = norm3(sub3(Lp, hp));
+                        const int lr = cast_mask<SMEM>(P, rdist, add3(hp, mul3s(tl, 0.001f)), tl, f2i(fadd(ld, 1.0f)),
+                                                       u.maxSteps, c2, a2, s2, steps, dummy, refills);
+                        res.cast |= 2u << i;
+                        if (lr != T_HIT) {
+                            const float nl = fmax0(dot3(hn, tl));
+                            const float fall = fdiv(fsub(R, ld), R);
+                            const float a = u.localLights[i][3];
+                            mr = fadd(mr, fmul(fmul(fmul(a, u.localLightColor[i][0]), nl), fall));
+                            mg = fadd(mg, fmul(fmul(fmul(a, u.localLightColor[i][1]), nl), fall));
+                            mb = fadd(mb, fmul(fmul(fmul(a, u.localLightColor[i][2]), nl), fall));
+                        } else {
+                            res.occ |= 2u << i;
+                        }
+                    }
+                }
+            }
+            word = __ldg(P.words + hit);
+        }
+        res.hit = pr == T_HIT ? hit : -1;
+        res.steps = steps;
+        res.mr = mr; res.mg = mg; res.mb = mb;
+        res.rgba = pack_color(u, pr == T_HIT, word, mr, mg, mb, res.primary_steps);
+        store_pixel(V.dbg, V.rgba, (uint64_t)py * V.width + px, res);
+    }
+    if (V.stats) {
+        unsigned rays = valid ? 1u + __popc(res.cast) : 0u;
+        unsigned hits = valid && res.hit >= 0 ? 1u : 0u;
+        unsigned pix = valid ? 1u : 0u;
+        unsigned long long s64 = valid ? (unsigned)res.steps : 0u;
+        unsigned long long r64 = refills;
+        for (int off = 16; off > 0; off >>= 1) {
+            s64 += __shfl_down_sync(0xffffffffu, s64, off);
+            r64 += __shfl_down_sync(0xffffffffu, r64, off);
+        }
+        rays = __reduce_add_sync(0xffffffffu, rays);
+        hits = __reduce_add_sync(0xffffffffu, hits);
+        pix = __reduce_add_sync(0xffffffffu, pix);
+        if ((threadIdx.x & 31) == 0) {
+            atomicAdd(V.stats + VRT_STAT_RAYS, (unsigned long long)rays);
+            atomicAdd(V.stats + VRT_STAT_STEPS, s64);
+            atomicAdd(V.stats + VRT_STAT_HITS, (unsigned long long)hits);
+            atomicAdd(V.stats + VRT_STAT_PIXELS, (unsigned long long)pix);
+            atomicAdd(V.stats + VRT_STAT_REFILLS, r64);
+        }
     }
 }
 
@@ -576,15 +771,19 @@ struct Tuning {
 };
 
 static Tuning tuning_of(const vrt_render_opts* o) {
-    Tuning t{8, 4, 8, 3};
+    Tuning t{8, 4, 8, 4};
     if (o) {
         if (o->tile_w > 0) t.tile_w = o->tile_w;
         if (o->tile_h > 0) t.tile_h = o->tile_h;
         if (o->refill_min > 0) t.refill_min = std::min(o->refill_min, 32);
-        if (o->blocks_per_sm > 0) t.blocks_per_sm = std::min(o->blocks_per_sm, 3);
+        if (o->blocks_per_sm > 0) t.blocks_per_sm = std::min(o->blocks_per_sm, 8);
     }
     return t;
 }
+
+// Region distances go to shared memory when they take at most this many bytes
+// (16 KiB for 512x256x512, 4 KiB for 256^3); larger worlds read them through L1.
+constexpr int kSmemRegionLimit = 32768;
 
 static int launch_mask(vrt_renderer* r, const vrt_world* w, const ViewDev* h_views, int nviews, int total_tiles,
                        const Tuning& t, const ViewDev* d_views, unsigned int* d_counter, cudaStream_t s) {
@@ -592,21 +791,51 @@ static int launch_mask(vrt_renderer* r, const vrt_world* w, const ViewDev* h_vie
     std::memset(&P, 0, sizeof(P));
     P.words = w->d_words;
     P.bricks = w->d_bricks;
-    P.regions = w->d_regions;
-    P.supers = w->d_supers;
+    P.bdist = w->d_bdist;
+    P.rdist = w->d_rdist;
     P.L = w->L;
     P.views = nviews == 1 ? nullptr : d_views;
     P.nviews = nviews;
     P.total_tiles = total_tiles;
-    P.tile_w = t.tile_w;
-    P.tile_h = t.tile_h;
-    P.refill_min = t.refill_min;
     P.tile_counter = d_counter;
     P.v0 = h_views[0];
+    const int region_bytes = w->L.RWp * w->L.RHp * w->L.RWp;
+    P.region_bytes16 = (region_bytes + 15) & ~15;
+    const bool smem_regions = P.region_bytes16 <= kSmemRegionLimit;
+    const size_t smem = (smem_regions ? P.region_bytes16 : 0) + sizeof(uint32_t) * NF * kThreads;
+    // 4 CTAs/SM caps registers at 64, 3 CTAs/SM at 85 (no spills); blocks_per_sm picks
+    auto kern = t.blocks_per_sm >= 4 ? (smem_regions ? render_mask_kernel<true, 4> : render_mask_kernel<false, 4>)
+                                     : (smem_regions ? render_mask_kernel<true, 3> : render_mask_kernel<false, 3>);
+    VRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    int per_sm = 0;
+    VRT_CUDA(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, kThreads, smem));
+    per_sm = std::max(1, std::min(per_sm, t.blocks_per_sm));
     VRT_CUDA(cudaMemsetAsync(d_counter, 0, sizeof(unsigned), s));
-    // persistent grid: blocks_per_sm CTAs of 8 warps per SM, never more warps than tiles
-    int blocks = std::max(1, std::min(r->num_sms * t.blocks_per_sm, (total_tiles + 7) / 8));
-    render_mask_kernel<<<blocks, 256, 0, s>>>(P);
+    // persistent grid: per_sm CTAs of 8 warps per SM, never more warps than tiles
+    const int blocks = std::max(1, std::min(r->num_sms * per_sm, (total_tiles + 7) / 8));
+    kern<<<blocks, kThreads, smem, s>>>(P);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+static int launch_mask_pixel(const vrt_world* w, const ViewDev& v, cudaStream_t s) {
+    MaskParams P;
+    std::memset(&P, 0, sizeof(P));
+    P.words = w->d_words;
+    P.bricks = w->d_bricks;
+    P.bdist = w->d_bdist;
+    P.rdist = w->d_rdist;
+    P.L = w->L;
+    P.nviews = 1;
+    P.v0 = v;
+    const int region_bytes = w->L.RWp * w->L.RHp * w->L.RWp;
+    P.region_bytes16 = (region_bytes + 15) & ~15;
+    const bool smem_regions = P.region_bytes16 <= kSmemRegionLimit;
+    const size_t smem = smem_regions ? P.region_bytes16 : 0;
+    auto kern = smem_regions ? render_mask_pixel_kernel<true> : render_mask_pixel_kernel<false>;
+    VRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    dim3 grid((v.width + 15) / 16, (v.height + 7) / 8);
+    kern<<<grid, 128, smem, s>>>(P);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
@@ -617,6 +846,9 @@ static void fill_view(ViewDev& v, const vrt_uniforms& u, int width, int height, 
     v.u = u;
     v.width = width;
     v.height = height;
+    v.tile_w = t.tile_w;
+    v.tile_h = t.tile_h;
+    v.refill_min = t.refill_min;
     v.tiles_x = (width + t.tile_w - 1) / t.tile_w;
     v.tile_begin = tile_begin;
     v.rgba = rgba;
@@ -675,7 +907,7 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
     if (width < 1 || height < 1 || width > 32768 || height > 32768)
         return set_error(VRT_EINVAL, "image %d x %d out of range", width, height);
     int kernel = opts ? opts->kernel : VRT_KERNEL_AUTO;
-    if (kernel == VRT_KERNEL_AUTO) kernel = w->has_depth_field ? VRT_KERNEL_WORD : VRT_KERNEL_BITMASK;
+    if (kernel == VRT_KERNEL_AUTO) kernel = w->has_depth_field ? VRT_KERNEL_WORD : VRT_KERNEL_MASK_PIXEL;
     if (kernel == VRT_KERNEL_BITMASK && w->has_depth_field)
         return set_error(VRT_ESTATE, "the world holds depth-field words, which only the word kernel follows");
     if (kernel == VRT_KERNEL_WORD) {
@@ -691,6 +923,14 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
         render_word_kernel<<<grid, 128, 0, S(stream)>>>(w->d_words, w->L, p);
         VRT_CUDA(cudaGetLastError());
         return VRT_OK;
+    }
+    if (kernel == VRT_KERNEL_MASK_PIXEL) {
+        if (w->has_depth_field)
+            return set_error(VRT_ESTATE, "the world holds depth-field words, which only the word kernel follows");
+        Tuning t = tuning_of(opts);
+        ViewDev v;
+        fill_view(v, *u, width, height, d_rgba, dbg, d_stats, t, 0);
+        return launch_mask_pixel(w, v, S(stream));
     }
     if (kernel != VRT_KERNEL_BITMASK) return set_error(VRT_EINVAL, "unknown kernel %d", kernel);
     Tuning t = tuning_of(opts);

@@ -34,11 +34,25 @@ struct Layout {
     int RW, RH;         // regions per axis (x/z, y): ceil(W/16), ceil(H/16)
     int SW, SH;         // super blocks per axis: ceil(W/64), ceil(H/64)
     int RWp, RHp;       // regions per axis padded to a multiple of 4 (= 4*SW, 4*SH)
+    int BWp, BHp;       // bricks per axis, padded (= 16*SW, 16*SH)
     uint64_t n_words;   // W*H*W
     uint64_t n_bricks;  // 64 * RWp*RHp*RWp
     uint64_t n_regions; // 64 * SW*SH*SW
     uint64_t n_supers;  // SW*SH*SW
 };
+
+// Empty-space distance fields (capped Chebyshev distance, in nodes, to the nearest
+// non-empty node; 0 = the node itself holds a solid voxel):
+//   brick distance: uint8 per brick, stored like the brick masks (node-major);
+//   region distance: uint8 per region, linear index rx + RWp*(ry + RHp*rz).
+// A node at distance d >= 1 has every node within Chebyshev radius d-1 empty, so the
+// cube of those nodes is a box a ray can cross without reading voxels.  Values are
+// capped (never larger than the truth), and recomputed whenever solids may be added.
+constexpr int kDistCap = 15;
+
+__host__ __device__ inline uint64_t region_linear(const Layout& L, int rx, int ry, int rz) {
+    return (uint64_t)rx + (uint64_t)L.RWp * ((uint64_t)ry + (uint64_t)L.RHp * rz);
+}
 
 __host__ __device__ inline uint64_t super_index(const Layout& L, int sx, int sy, int sz) {
     return (uint64_t)sx + (uint64_t)L.SW * ((uint64_t)sy + (uint64_t)L.SH * sz);
@@ -62,6 +76,10 @@ struct vrt_world {
     uint64_t* d_bricks = nullptr;
     uint64_t* d_regions = nullptr;
     uint64_t* d_supers = nullptr;
+    uint8_t* d_bdist = nullptr;     // brick distance field (node-major, n_bricks)
+    uint8_t* d_rdist = nullptr;     // region distance field (linear, RWp*RHp*RWp)
+    uint8_t* d_tmp_a = nullptr;     // scratch of the distance passes (n_bricks each)
+    uint8_t* d_tmp_b = nullptr;
     int* d_flag = nullptr;          // has-depth-field flag written by the mask kernels
     int has_depth_field = 0;        // host copy (as of the last sync)
     uint64_t device_bytes = 0;

@@ -27,6 +27,8 @@ Layout make_layout(int W, int H) {
     L.SH = (H + 63) / 64;
     L.RWp = 4 * L.SW;
     L.RHp = 4 * L.SH;
+    L.BWp = 16 * L.SW;
+    L.BHp = 16 * L.SH;
     L.n_words = (uint64_t)W * H * W;
     L.n_supers = (uint64_t)L.SW * L.SH * L.SW;
     L.n_regions = 64 * L.n_supers;
@@ -97,6 +99,72 @@ __global__ void parent_mask_kernel(const uint64_t* __restrict__ child, uint64_t*
 
 static inline unsigned blocks_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// One 1-D pass of the capped Chebyshev distance transform over the box
+// [x0,x0+nx) x [y0,y0+ny) x [z0,z0+nz) of the brick (level 0) or region (level 1) grid:
+//   out(p) = min over |k| <= cap of max(|k|, in(p + k e_axis)),
+// where in() of the first pass is 0 for a non-empty node and cap+1 for an empty one, and
+// nodes outside the padded grid are empty.  Three passes (x, y, z) give the L-inf distance.
+__global__ void cheb_pass_kernel(const uint64_t* __restrict__ occ, const uint8_t* __restrict__ in,
+                                 uint8_t* __restrict__ out, Layout L, int level, int axis, int x0, int y0, int z0,
+                                 int nx, int ny, int nz, int first) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)nx * ny * nz) return;
+    const int x = x0 + (int)(t % nx), y = y0 + (int)((t / nx) % ny), z = z0 + (int)(t / ((uint64_t)nx * ny));
+    const int DX = level == 0 ? L.BWp : L.RWp, DY = level == 0 ? L.BHp : L.RHp;
+    const int cap = kDistCap;
+    int best = cap + 1;
+    for (int k = -cap; k <= cap; k++) {
+        int qx = x + (axis == 0 ? k : 0), qy = y + (axis == 1 ? k : 0), qz = z + (axis == 2 ? k : 0);
+        if (qx < 0 || qy < 0 || qz < 0 || qx >= DX || qy >= DY || qz >= DX) continue;
+        int v;
+        if (first) {
+            uint64_t oi = level == 0 ? brick_index(L, qx, qy, qz) : region_index(L, qx, qy, qz);
+            v = occ[oi] != 0 ? 0 : cap + 1;
+        } else {
+            v = in[level == 0 ? brick_index(L, qx, qy, qz) : region_linear(L, qx, qy, qz)];
+        }
+        int a = k < 0 ? -k : k;
+        best = min(best, max(a, v));
+    }
+    out[level == 0 ? brick_index(L, x, y, z) : region_linear(L, x, y, z)] = (uint8_t)min(best, cap);
+}
+
+static int dist_passes(vrt_world* w, int level, int bx0, int by0, int bz0, int bx1, int by1, int bz1,
+                       cudaStream_t s) {
+    const Layout& L = w->L;
+    const int cap = kDistCap;
+    const int DX = level == 0 ? L.BWp : L.RWp, DY = level == 0 ? L.BHp : L.RHp;
+    auto clampbox = [&](int& a0, int& a1, int lim) { a0 = std::max(a0, 0); a1 = std::min(a1, lim); };
+    // the z pass writes B; the y pass must cover B grown by cap in z; the x pass B grown in y and z
+    int X0 = bx0, X1 = bx1, Y0 = by0, Y1 = by1, Z0 = bz0, Z1 = bz1;
+    clampbox(X0, X1, DX); clampbox(Y0, Y1, DY); clampbox(Z0, Z1, DX);
+    if (X0 >= X1 || Y0 >= Y1 || Z0 >= Z1) return VRT_OK;
+    int ya0 = Y0 - cap, ya1 = Y1 + cap, za0 = Z0 - cap, za1 = Z1 + cap;
+    clampbox(ya0, ya1, DY); clampbox(za0, za1, DX);
+    const uint64_t* occ = level == 0 ? w->d_bricks : w->d_regions;
+    uint8_t* dst = level == 0 ? w->d_bdist : w->d_rdist;
+    uint64_t n = (uint64_t)(X1 - X0) * (ya1 - ya0) * (za1 - za0);
+    cheb_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(occ, nullptr, w->d_tmp_a, L, level, 0, X0, ya0, za0, X1 - X0,
+                                                        ya1 - ya0, za1 - za0, 1);
+    n = (uint64_t)(X1 - X0) * (Y1 - Y0) * (za1 - za0);
+    cheb_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(occ, w->d_tmp_a, w->d_tmp_b, L, level, 1, X0, Y0, za0,
+                                                        X1 - X0, Y1 - Y0, za1 - za0, 0);
+    n = (uint64_t)(X1 - X0) * (Y1 - Y0) * (Z1 - Z0);
+    cheb_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(occ, w->d_tmp_b, dst, L, level, 2, X0, Y0, Z0, X1 - X0,
+                                                        Y1 - Y0, Z1 - Z0, 0);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+// Distances of every brick within kDistCap bricks of the changed brick box, and of all
+// regions (a few thousand to a few hundred thousand bytes).
+static int refresh_distances(vrt_world* w, int bx0, int by0, int bz0, int bx1, int by1, int bz1, cudaStream_t s) {
+    const int cap = kDistCap;
+    int st = dist_passes(w, 0, bx0 - cap, by0 - cap, bz0 - cap, bx1 + cap, by1 + cap, bz1 + cap, s);
+    if (st) return st;
+    return dist_passes(w, 1, 0, 0, 0, w->L.RWp, w->L.RHp, w->L.RWp, s);
+}
+
 int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int z1, cudaStream_t s) {
     const Layout& L = w->L;
     x0 = std::max(x0, 0); y0 = std::max(y0, 0); z0 = std::max(z0, 0);
@@ -118,7 +186,7 @@ int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int 
     parent_mask_kernel<<<blocks_for(ns, 256), 256, 0, s>>>(w->d_regions, w->d_supers, sx0, sy0, sz0, sx1 - sx0,
                                                            sy1 - sy0, sz1 - sz0, L, 2);
     VRT_CUDA(cudaGetLastError());
-    return VRT_OK;
+    return refresh_distances(w, bx0, by0, bz0, bx1, by1, bz1, s);
 }
 
 int refresh_masks(vrt_world* w, uint64_t first, uint64_t count, cudaStream_t s) {
@@ -164,7 +232,7 @@ struct DepthOff {
     float dist;
     int8_t x, y, z, pad;
 };
-__constant__ DepthOff c_depth_offs[1024];
+__constant__ DepthOff c_depth_offs[1536];  // 1413 offsets of the radius-7 sphere have d > -6
 __constant__ int c_depth_count;
 static std::once_flag g_depth_once;
 static int g_depth_count = 0;
@@ -306,16 +374,24 @@ int vrt_world_create(int32_t width, int32_t height, vrt_world** out) {
     vrt_world* w = new vrt_world();
     w->L = make_layout(width, height);
     cudaGetDevice(&w->device);
-    uint64_t bytes = w->L.n_words * 4 + (w->L.n_bricks + w->L.n_regions + w->L.n_supers) * 8 + 256;
+    uint64_t bytes = w->L.n_words * 4 + (w->L.n_bricks + w->L.n_regions + w->L.n_supers) * 8 + 3 * w->L.n_bricks +
+                     (uint64_t)w->L.RWp * w->L.RHp * w->L.RWp + 256;
     cudaError_t e = cudaMalloc(&w->d_words, w->L.n_words * 4);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_bricks, w->L.n_bricks * 8);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_regions, w->L.n_regions * 8);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_supers, w->L.n_supers * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_bdist, w->L.n_bricks);
+    const uint64_t rbytes = ((uint64_t)w->L.RWp * w->L.RHp * w->L.RWp + 15) & ~(uint64_t)15;  // staged as uint4
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_rdist, rbytes);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_tmp_a, w->L.n_bricks);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_tmp_b, w->L.n_bricks);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(w->d_words, 0xFF, w->L.n_words * 4);  // air = -1 (render.cpp:349-351)
     if (e == cudaSuccess) e = cudaMemset(w->d_bricks, 0, w->L.n_bricks * 8);
     if (e == cudaSuccess) e = cudaMemset(w->d_regions, 0, w->L.n_regions * 8);
     if (e == cudaSuccess) e = cudaMemset(w->d_supers, 0, w->L.n_supers * 8);
+    if (e == cudaSuccess) e = cudaMemset(w->d_bdist, kDistCap, w->L.n_bricks);  // an all-air world
+    if (e == cudaSuccess) e = cudaMemset(w->d_rdist, kDistCap, rbytes);
     if (e == cudaSuccess) e = cudaMemset(w->d_flag, 0, sizeof(int));
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
@@ -335,6 +411,10 @@ int vrt_world_destroy(vrt_world* w) {
     cudaFree(w->d_bricks);
     cudaFree(w->d_regions);
     cudaFree(w->d_supers);
+    cudaFree(w->d_bdist);
+    cudaFree(w->d_rdist);
+    cudaFree(w->d_tmp_a);
+    cudaFree(w->d_tmp_b);
     cudaFree(w->d_flag);
     delete w;
     return VRT_OK;

@@ -26,8 +26,8 @@ MAX_LOCAL_LIGHTS = 16
 OK = 0
 EINVAL, ECUDA, ENOMEM, ERANGE, ETIMEOUT, EBUDGET, ENOTFOUND, ESTATE = -1, -2, -3, -4, -5, -6, -7, -8
 
-KERNEL_AUTO, KERNEL_WORD, KERNEL_BITMASK = 0, 1, 2
-STAT_RAYS, STAT_STEPS, STAT_HITS, STAT_PIXELS, STAT_COUNT = 0, 1, 2, 3, 8
+KERNEL_AUTO, KERNEL_WORD, KERNEL_BITMASK, KERNEL_MASK_PIXEL = 0, 1, 2, 3
+STAT_RAYS, STAT_STEPS, STAT_HITS, STAT_PIXELS, STAT_REFILLS, STAT_SLOW, STAT_FAST, STAT_COUNT = 0, 1, 2, 3, 4, 5, 6, 8
 REQ_RENDER, REQ_EDIT = 0, 1
 
 
