@@ -223,6 +223,19 @@ typedef struct vrt_view {
 int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count,
                      const vrt_render_opts* opts, void* stream);
 
+/* vrt_render_batch for callers that may not allocate device memory -- for example a
+ * plugin whose host application owns every device allocation, or a frame loop that
+ * cannot afford cudaMalloc's implicit device synchronisation.  It has no counterpart in
+ * the reference.  It takes no renderer: its scratch (the tile counter and the view table)
+ * lives in a static device array of the library, about 46 KiB per GPU, so it calls no
+ * cudaMalloc or cudaFree.  At most VRT_NOALLOC_MAX_VIEWS views per call (more:
+ * VRT_ERANGE).  The first call on each device looks up the array's device address
+ * (cudaGetSymbolAddress) with that device current; make that first call before any stream
+ * capture.  Every call shares the one array and resets its counter, so calls that overlap
+ * on the GPU (other streams, other threads) race: order them on one stream. */
+#define VRT_NOALLOC_MAX_VIEWS 64
+int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, const vrt_render_opts* opts, void* stream);
+
 /* A captured CUDA graph of vrt_render_batch over a fixed view list; replay with
  * vrt_batch_graph_launch.  Uniform or image-pointer changes need a new graph. */
 typedef struct vrt_batch_graph vrt_batch_graph;

@@ -19,6 +19,7 @@
 #include <algorithm>
 #include <climits>
 #include <cstring>
+#include <mutex>
 #include <vector>
 
 #include "shade_common.cuh"
@@ -1090,3 +1091,71 @@ int vrt_probe_l2_read_gbs(uint64_t bytes, int32_t iters, double* gbs_out) {
 }
 
 }  // extern "C"
+
+// ====================================================================== batch without allocation
+
+// vrt_render_batch_noalloc keeps its scratch -- the tile counter the persistent warps
+// draw tiles from, and the table of views they read -- in this file-scope array instead
+// of device memory that a renderer allocates.  Every GPU that loads the library holds it
+// (about 46 KiB) until the process exits.  Host code cannot use the array's name as a
+// device address: the address comes from cudaGetSymbolAddress, once per device, below.
+constexpr int kNoAllocMaxViews = VRT_NOALLOC_MAX_VIEWS;
+constexpr size_t kNoAllocCounterBytes = 256;
+constexpr size_t kNoAllocBytes = kNoAllocCounterBytes + sizeof(ViewDev) * kNoAllocMaxViews;
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocBytes];
+
+constexpr int kNoAllocMaxDevices = 64;
+static std::mutex g_noalloc_mutex;
+static void* g_noalloc_address[kNoAllocMaxDevices];
+
+// Device address of the scratch array on the current device, looked up on the first call
+// made with that device current.
+static int noalloc_scratch(void** out) {
+    int dev = 0;
+    VRT_CUDA(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return set_error(VRT_ERANGE, "device %d beyond %d", dev, kNoAllocMaxDevices);
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_address[dev]) {
+        void* p = nullptr;
+        cudaError_t e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess) return cuda_error(e, "cudaGetSymbolAddress(g_noalloc_scratch)");
+        g_noalloc_address[dev] = p;
+    }
+    *out = g_noalloc_address[dev];
+    return VRT_OK;
+}
+
+extern "C" int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, const vrt_render_opts* opts,
+                                        void* stream) {
+    if (!views || count < 1) return set_error(VRT_EINVAL, "empty batch");
+    if (count > kNoAllocMaxViews)
+        return set_error(VRT_ERANGE, "%d views exceed the %d the static scratch holds; split the batch", count,
+                         kNoAllocMaxViews);
+    const vrt_world* w = views[0].world;
+    if (!w) return set_error(VRT_EINVAL, "view 0 has no world");
+    if (w->has_depth_field) return set_error(VRT_ESTATE, "batched rendering needs a world without depth-field words");
+    const Tuning t = tuning_of(opts);
+    ViewDev hv[kNoAllocMaxViews];  // host copy of the view table, on the stack
+    int tiles = 0;
+    for (int i = 0; i < count; i++) {
+        const vrt_view& v = views[i];
+        if (v.world != w) return set_error(VRT_EINVAL, "view %d renders another world; one batch = one world", i);
+        if (!v.d_rgba || v.width < 1 || v.height < 1 || v.width > 32768 || v.height > 32768)
+            return set_error(VRT_EINVAL, "view %d: bad image", i);
+        int st = check_uniforms(&v.uniforms);
+        if (st) return st;
+        fill_view(hv[i], v.uniforms, v.width, v.height, v.d_rgba, nullptr, v.d_stats, t, tiles);
+        tiles += tiles_of(v.width, v.height, t);
+    }
+    void* scratch = nullptr;
+    int st = noalloc_scratch(&scratch);
+    if (st) return st;
+    unsigned int* d_counter = reinterpret_cast<unsigned int*>(scratch);
+    ViewDev* d_views = reinterpret_cast<ViewDev*>(static_cast<unsigned char*>(scratch) + kNoAllocCounterBytes);
+    if (count > 1)  // pageable source: the copy is staged before the call returns
+        VRT_CUDA(cudaMemcpyAsync(d_views, hv, sizeof(ViewDev) * count, cudaMemcpyHostToDevice, S(stream)));
+    vrt_renderer shape;  // only its SM count is read by the launch
+    VRT_CUDA(cudaGetDevice(&shape.device));
+    VRT_CUDA(cudaDeviceGetAttribute(&shape.num_sms, cudaDevAttrMultiProcessorCount, shape.device));
+    return launch_mask(&shape, w, hv, count, tiles, t, d_views, d_counter, S(stream));  // zeroes the counter
+}

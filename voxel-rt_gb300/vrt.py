@@ -29,6 +29,7 @@ EINVAL, ECUDA, ENOMEM, ERANGE, ETIMEOUT, EBUDGET, ENOTFOUND, ESTATE = -1, -2, -3
 KERNEL_AUTO, KERNEL_WORD, KERNEL_BITMASK, KERNEL_MASK_PIXEL = 0, 1, 2, 3
 STAT_RAYS, STAT_STEPS, STAT_HITS, STAT_PIXELS, STAT_REFILLS, STAT_SLOW, STAT_FAST, STAT_COUNT = 0, 1, 2, 3, 4, 5, 6, 8
 REQ_RENDER, REQ_EDIT = 0, 1
+NOALLOC_MAX_VIEWS = 64
 
 
 class VrtError(RuntimeError):
@@ -173,6 +174,7 @@ SIGNATURES = {
                         C.POINTER(RenderOpts), _P]),
     "vrt_render_to_host": (_I, [_P, _P, C.POINTER(Uniforms), _I, _I, _P, C.POINTER(RenderOpts), _P]),
     "vrt_render_batch": (_I, [_P, C.POINTER(View), _I, C.POINTER(RenderOpts), _P]),
+    "vrt_render_batch_noalloc": (_I, [C.POINTER(View), _I, C.POINTER(RenderOpts), _P]),
     "vrt_batch_graph_create": (_I, [_P, C.POINTER(View), _I, C.POINTER(RenderOpts), _P, C.POINTER(_P)]),
     "vrt_batch_graph_launch": (_I, [_P, _P]),
     "vrt_batch_graph_destroy": (_I, [_P]),
