@@ -181,7 +181,7 @@ def main():
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true", help="skip the batched / served / CPU legs")
     ap.add_argument("--kernel", default="pixel", choices=["pixel", "mask", "word"])
-    ap.add_argument("--tile", default="8x4")
+    ap.add_argument("--tile", default="8x16")
     ap.add_argument("--refill", type=int, default=8)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     args = ap.parse_args()
@@ -223,10 +223,20 @@ def main():
     W, H = sc.width, sc.height
     img = torch.empty(W * H * 4, dtype=torch.uint8, device=dev)
     stats = torch.zeros(vrt.STAT_COUNT, dtype=torch.int64, device=dev)
-    r.render(world, sc.uniforms, W, H, img.data_ptr(), None, stats.data_ptr(), opts, sh)
+    # counting frames: exact shader step accounting (the reference's DDA iterations, S), and
+    # the iterations the timed path performs (rays that cannot hit end early)
+    exact_opts = vrt.RenderOpts.from_buffer_copy(opts)
+    exact_opts.exact_steps = 1
+    r.render(world, sc.uniforms, W, H, img.data_ptr(), None, stats.data_ptr(), exact_opts, sh)
     torch.cuda.synchronize()
     st = stats.cpu().numpy()
     rays, steps, hits, pixels = (int(st[i]) for i in range(4))
+    stats.zero_()
+    r.render(world, sc.uniforms, W, H, img.data_ptr(), None, stats.data_ptr(), opts, sh)
+    torch.cuda.synchronize()
+    st_fast = stats.cpu().numpy()
+    assert int(st_fast[0]) == rays and int(st_fast[2]) == hits, "ray counts differ between counting frames"
+    steps_performed = int(st_fast[1])
     flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
 
     for _ in range(args.warmup):
@@ -280,14 +290,17 @@ def main():
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": load_traffic(kname, "full"), "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": algo_bytes, "kernel": kname,
-                "note": "effective bytes: one 4-byte word per DDA step as the shader reads; the mask kernel reads "
-                        "far fewer physical bytes (traffic)"}
+                "note": "effective bytes: one 4-byte word per DDA iteration of the shader (S counted exactly on the "
+                        "device, equal to the oracle's) + the colour word per primary hit + the RGBA8 store; the mask "
+                        "kernels read far fewer physical bytes (traffic) and end rays that cannot hit early "
+                        "(config.dda_steps_performed)"}
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded terrain, seed 2)",
         "config": {"workload": sc.workload, "rays_per_frame": rays, "dda_steps_per_frame": steps,
+                   "dda_steps_performed": steps_performed, "box_lookups": int(st_fast[4]),
                    "primary_hits": hits, "pixels": pixels, "kernel": kname, "tile": args.tile,
                    "refill_min": args.refill, "l2": "flushed before every timed frame (256 MiB write)",
                    "parallelism": f"replicas x{world_size}"},

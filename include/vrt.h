@@ -104,11 +104,19 @@ typedef struct vrt_debug_out {
 #define VRT_KERNEL_BITMASK 2  /* occupancy-mask traversal, persistent ray refill    */
 #define VRT_KERNEL_MASK_PIXEL 3 /* occupancy-mask traversal, one thread per pixel     */
 
+/* Step accounting.  The occupancy-mask kernels end a ray as soon as its path provably
+ * holds no solid voxel: its cell lies beyond the bounding box of the world's solid voxels
+ * along an axis it moves away from (or parallel to).  Such a ray misses whatever path it
+ * takes, so every pixel, cast bit and occlusion bit is unchanged; only the number of DDA
+ * iterations performed drops.  Those counts (VRT_STAT_STEPS, the steps / primary_steps
+ * debug outputs, the viewDepthField step view) equal the shader's exactly whenever they are
+ * asked for: exact_steps = 1, a steps or primary_steps debug output, or viewDepthField. */
 typedef struct vrt_render_opts {
     int32_t kernel;          /* VRT_KERNEL_*                                        */
-    int32_t tile_w, tile_h;  /* ray tile of the mask kernel (0 = default 8x4)       */
-    int32_t refill_min;      /* mask kernel: refill idle lanes once this many are idle (0 = default) */
-    int32_t blocks_per_sm;   /* mask kernel: resident CTAs per SM (0 = default)     */
+    int32_t tile_w, tile_h;  /* ray tile (0 = kernel default: 8x16 tile kernel, 8x4 persistent) */
+    int32_t refill_min;      /* persistent kernel: lanes parked before a slow phase (0 = default) */
+    int32_t blocks_per_sm;   /* persistent kernel: resident CTAs per SM (0 = default) */
+    int32_t exact_steps;     /* 1: count every DDA iteration of the shader, no early miss */
 } vrt_render_opts;
 
 typedef struct vrt_world vrt_world;

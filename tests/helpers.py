@@ -47,8 +47,10 @@ def fcolor_from_outputs(words, hit, shade, primary_steps=None, depth_view=False)
 
 
 def gpu_render(world: vrt.World, u: vrt.Uniforms, width: int, height: int, kernel: int = vrt.KERNEL_AUTO,
-               tile=None, refill_min: int = 0, renderer: vrt.Renderer | None = None):
-    """Render through the C ABI with every debug output; returns numpy arrays + stats."""
+               tile=None, refill_min: int = 0, renderer: vrt.Renderer | None = None, debug: bool = True,
+               exact_steps: int = 0):
+    """Render through the C ABI; with debug=True every debug output is requested (which
+    makes step accounting exact), with debug=False only the image and the counters."""
     import torch
     dev = torch.device("cuda")
     n = width * height
@@ -61,9 +63,10 @@ def gpu_render(world: vrt.World, u: vrt.Uniforms, width: int, height: int, kerne
     shade = torch.zeros(n * 3, dtype=torch.float32, device=dev)
     stats = torch.zeros(vrt.STAT_COUNT, dtype=torch.int64, device=dev)
     dbg = vrt.DebugOut(hit.data_ptr(), cast.data_ptr(), occ.data_ptr(), steps.data_ptr(), psteps.data_ptr(),
-                       shade.data_ptr())
+                       shade.data_ptr()) if debug else None
     opts = vrt.RenderOpts()
     opts.kernel = kernel
+    opts.exact_steps = exact_steps
     if tile:
         opts.tile_w, opts.tile_h = tile
     opts.refill_min = refill_min

@@ -68,6 +68,23 @@ def test_full_world_reduced_frame(cuda, oracle, full_world, kernel):
     assert (o["cast"] > 1).sum() > 0  # local lights are cast
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_fast_mode_images_are_exact(cuda, oracle, full_world, kernel):
+    """Without step outputs the mask kernels end rays that cannot hit early: the image,
+    rays, hits and pixels stay exactly the oracle's; with exact_steps the steps do too."""
+    sc = full_world
+    o = oracle.render(sc.words, sc.W, sc.H, sc.uniforms, 480, 270)
+    w = make_world(sc.words, sc.W, sc.H)
+    g = gpu_render(w, sc.uniforms, 480, 270, kernel=kernel, debug=False)
+    assert np.array_equal(g["rgba"], o["rgba"])
+    t = o["totals"]
+    assert [int(v) for v in g["stats"][[0, 2, 3]]] == [t["rays"], t["hits"], t["pixels"]]
+    if kernel != vrt.KERNEL_WORD:
+        assert int(g["stats"][vrt.STAT_STEPS]) < t["steps"]  # rays that cannot hit ended early
+    e = gpu_render(w, sc.uniforms, 480, 270, kernel=kernel, debug=False, exact_steps=1)
+    assert np.array_equal(e["rgba"], o["rgba"]) and int(e["stats"][vrt.STAT_STEPS]) == t["steps"]
+
+
 def test_full_world_1080p_rows(cuda, oracle, full_world):
     """The full 1920x1080 frame on the GPU; every 24th row checked against the oracle."""
     sc = full_world
@@ -130,6 +147,18 @@ def test_tile_shapes_and_refill_are_invisible(cuda, oracle, small):
             g = gpu_render(w, sc.uniforms, sc.width, sc.height, kernel=vrt.KERNEL_BITMASK, tile=tile,
                            refill_min=refill)
             assert_same_frame(o, g)
+
+
+def test_tile_kernel_tile_shapes_are_invisible(cuda, oracle, full_world):
+    sc = full_world
+    u = sc.uniforms
+    o = oracle.render(sc.words, sc.W, sc.H, u, 200, 113)
+    w = make_world(sc.words, sc.W, sc.H)
+    for tile in [(16, 8), (32, 4), (8, 16), (8, 4), (32, 1), (8, 8), (64, 2), (128, 1)]:
+        g = gpu_render(w, u, 200, 113, kernel=vrt.KERNEL_MASK_PIXEL, tile=tile)
+        assert_same_frame(o, g)
+    with pytest.raises(vrt.VrtError):
+        gpu_render(w, u, 16, 16, kernel=vrt.KERNEL_MASK_PIXEL, tile=(5, 3))
 
 
 @pytest.mark.parametrize("dims", [(37, 21), (70, 65), (130, 8)])

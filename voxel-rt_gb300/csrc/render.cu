@@ -180,6 +180,7 @@ struct ViewDev {
     int tile_begin;  // first global tile of this view
     int tile_w, tile_h;
     int refill_min;  // lanes parked before a warp runs its slow phase (tile's view decides)
+    int exact;       // 1: step every ray to its end (step counts asked for); 0: end rays that cannot hit
     uint8_t* rgba;
     vrt_debug_out dbg;
     unsigned long long* stats;
@@ -190,6 +191,7 @@ struct MaskParams {
     const uint64_t* bricks;
     const uint8_t* bdist;
     const uint8_t* rdist;
+    const int* aabb;       // solid bounding box: min x,y,z, max x,y,z (never smaller than the truth)
     Layout L;
     const ViewDev* views;  // nviews entries (device); NULL when nviews == 1 (v0 is used)
     int nviews;
@@ -244,13 +246,22 @@ __device__ __forceinline__ int start_ray(Ray& r, V3 o, V3 d, int n, int maxSteps
     return r.rem;
 }
 
+// A ray in cell c cannot hit anything if, along some axis, c lies beyond the solid
+// bounding box and the ray moves away from it or parallel to it: every later cell stays
+// beyond the box along that axis.
+__device__ __forceinline__ bool beyond_solids(const int* bb, int cx, int cy, int cz, int sx, int sy, int sz) {
+    return (cx < __ldg(bb + 0) && sx <= 0) || (cy < __ldg(bb + 1) && sy <= 0) || (cz < __ldg(bb + 2) && sz <= 0) ||
+           (cx > __ldg(bb + 3) && sx >= 0) || (cy > __ldg(bb + 4) && sy >= 0) || (cz > __ldg(bb + 5) && sz >= 0);
+}
+
 // The parked step moved the ray into cell c outside its box: bound the largest known
 // box around c from the distance fields, or load the brick's voxel bits.
 template <bool SMEM>
-__device__ __forceinline__ int refill(Ray& r, const MaskParams& P, const uint8_t* rdist) {
+__device__ __forceinline__ int refill(Ray& r, const MaskParams& P, const uint8_t* rdist, const int* bb, bool exact) {
     const Layout& L = P.L;
     if ((unsigned)r.cx >= (unsigned)L.W || (unsigned)r.cy >= (unsigned)L.H || (unsigned)r.cz >= (unsigned)L.W)
         return T_MISS;  // getVoxelIndex == -1 (fshader.glsl:123-125)
+    if (!exact && beyond_solids(bb, r.cx, r.cy, r.cz, r.sx, r.sy, r.sz)) return T_MISS;
     const int rx = r.cx >> 4, ry = r.cy >> 4, rz = r.cz >> 4;
     const uint64_t rl = region_linear(L, rx, ry, rz);
     const int dr = SMEM ? (int)rdist[rl] : (int)__ldg(rdist + rl);
@@ -318,7 +329,7 @@ __global__ void __launch_bounds__(kThreads, MINB) render_mask_kernel(const __gri
         n_slow++;
         if (mode == M_BOX) {
             LSU(F_ST_REFILLS) += 1u;
-            const int t = refill<SMEM>(r, P, rdist);
+            const int t = refill<SMEM>(r, P, rdist, P.aabb, view_of(P, (int)LSU(F_VID)).exact != 0);
             if (t == T_LIVE) {
                 if (r.la == 0) r.tx = fadd(r.tx, r.dx);
                 else if (r.la == 1) r.ty = fadd(r.ty, r.dy);
@@ -576,52 +587,153 @@ __global__ void __launch_bounds__(kThreads, MINB) render_mask_kernel(const __gri
 #undef LSF
 }
 
-// ---------------------------------------------------------------- mask kernel, one thread per pixel
+// ---------------------------------------------------------------- tile kernel, one thread per pixel
 
-// castRay (fshader.glsl:59-129) over the occupancy hierarchy: the same per-cell adds and
-// decisions as the shader, memory read only when the ray leaves its known box.
+// Where a ray stands inside its known box.  Per axis: k = further steps along that axis
+// that stay inside the box (the step that makes k negative leaves it), e = the cell
+// coordinate that step reaches, so the cell is always e - s*(k+1).  An axis the ray does
+// not move along (s == 0) has k = INT_MAX and e = its fixed cell.
+struct BoxRay {
+    float tx, ty, tz;
+    float dx, dy, dz;
+    int kx, ky, kz;
+    int ex, ey, ez;
+    int sx, sy, sz;
+    int left;        // DDA iterations left, minus one: negative once the cap is used up
+    int bi;          // bit of the current cell in m (valid while m != 0)
+    uint64_t m;      // voxel bits of the current brick, 0 inside an empty box
+};
+
+__device__ __forceinline__ void set_axis(int c, int s, int lo, int hi, int& k, int& e) {
+    if (s > 0) { k = hi - 1 - c; e = hi; }
+    else if (s < 0) { k = c - lo; e = lo - 1; }
+    else { k = INT_MAX; e = c; }
+}
+
+// The ray stands in cell c, outside any known box: bound the largest empty box around
+// c from the distance fields, or load c's brick.  Returns T_LIVE, T_HIT (c is solid) or
+// T_MISS (c is outside the world).
 template <bool SMEM>
-__device__ __forceinline__ int cast_mask(const MaskParams& P, const uint8_t* rdist, V3 o, V3 d, int n, int maxSteps,
-                                         float& cd, int& axis, int& sgn, int& steps, int32_t& hit_index,
-                                         unsigned& refills) {
-    Ray r;
-    const int n0 = start_ray(r, o, d, n, maxSteps);
+__device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, const MaskParams& P,
+                                         const uint8_t* rdist, const int* bb, bool exact) {
+    const Layout& L = P.L;
+    if ((unsigned)cx >= (unsigned)L.W || (unsigned)cy >= (unsigned)L.H || (unsigned)cz >= (unsigned)L.W)
+        return T_MISS;  // getVoxelIndex == -1 (fshader.glsl:123-125)
+    if (!exact && beyond_solids(bb, cx, cy, cz, r.sx, r.sy, r.sz)) return T_MISS;
+    const int rx = cx >> 4, ry = cy >> 4, rz = cz >> 4;
+    const uint64_t rl = region_linear(L, rx, ry, rz);
+    const int dr = SMEM ? (int)rdist[rl] : (int)__ldg(rdist + rl);
+    int lox, loy, loz, hix, hiy, hiz;
+    uint64_t m = 0;
+    if (dr > 0) {  // every region within Chebyshev radius dr-1 is empty
+        const int k = dr - 1;
+        lox = (rx - k) << 4; loy = (ry - k) << 4; loz = (rz - k) << 4;
+        hix = (rx + k + 1) << 4; hiy = (ry + k + 1) << 4; hiz = (rz + k + 1) << 4;
+    } else {
+        const int bx = cx >> 2, by = cy >> 2, bz = cz >> 2;
+        const uint64_t bidx = brick_index(L, bx, by, bz);
+        m = __ldg(P.bricks + bidx);
+        const int db = __ldg(P.bdist + bidx);
+        const int k = m ? 0 : max(db, 1) - 1;
+        lox = (bx - k) << 2; loy = (by - k) << 2; loz = (bz - k) << 2;
+        hix = (bx + k + 1) << 2; hiy = (by + k + 1) << 2; hiz = (bz + k + 1) << 2;
+    }
+    lox = max(lox, 0); loy = max(loy, 0); loz = max(loz, 0);
+    hix = min(hix, L.W); hiy = min(hiy, L.H); hiz = min(hiz, L.W);
+    set_axis(cx, r.sx, lox, hix, r.kx, r.ex);
+    set_axis(cy, r.sy, loy, hiy, r.ky, r.ey);
+    set_axis(cz, r.sz, loz, hiz, r.kz, r.ez);
+    r.m = m;
+    r.bi = (cx & 3) | ((cy & 3) << 2) | ((cz & 3) << 4);
+    return ((m >> r.bi) & 1) ? T_HIT : T_LIVE;
+}
+
+// castRay (fshader.glsl:59-129) over the occupancy hierarchy.  Every iteration makes the
+// shader's comparison and its one intersect add, in the shader's order; memory is read
+// only when the ray leaves its known box.  On a hit, cd / axis / sgn / cell describe the
+// last step (currDist, hitNormal, the voxel).
+template <bool SMEM>
+__device__ __forceinline__ int cast_box(const MaskParams& P, const uint8_t* rdist, const int* bb, bool exact, V3 o,
+                                        V3 d, int n, int maxSteps, float& cd, int& axis, int& sgn, int& steps,
+                                        int32_t& hit_index, unsigned& refills) {
+    RaySetup s;
+    ray_setup(o, d, s);
+    BoxRay r;
+    r.tx = s.tx; r.ty = s.ty; r.tz = s.tz;
+    r.dx = s.dx; r.dy = s.dy; r.dz = s.dz;
+    r.sx = s.sx; r.sy = s.sy; r.sz = s.sz;
+    const int n0 = max(0, min(n, maxSteps));
+    if (n0 == 0) return T_MISS;
+    r.left = n0 - 1;
+    // no box yet: the first step along any axis (even one with s == 0) triggers a lookup
+    r.kx = 0; r.ky = 0; r.kz = 0;
+    r.ex = s.cx + s.sx; r.ey = s.cy + s.sy; r.ez = s.cz + s.sz;
+    r.m = 0;
+    r.bi = 0;
     int result = T_MISS;
-    while (r.rem != 0) {
-        r.rem -= 1;
+    for (;;) {
         const bool bx = (r.tx < r.ty) & (r.tx < r.tz);
-        const bool by = (!bx) & (r.ty < r.tx) & (r.ty < r.tz);
+        const bool by = (r.ty < r.tx) & (r.ty < r.tz);  // false whenever bx holds, NaN included
         const bool bz = !(bx | by);
-        if (bx) r.cx += r.sx;
-        if (by) r.cy += r.sy;
-        if (bz) r.cz += r.sz;
-        const bool out = (r.cx == r.ex) | (r.cy == r.ey) | (r.cz == r.ez);
-        int t = T_LIVE;
-        if (out) {
-            refills++;
-            t = refill<SMEM>(r, P, rdist);
-        } else {
-            const int bit = (r.cx & 3) | ((r.cy & 3) << 2) | ((r.cz & 3) << 4);
-            if ((r.m >> bit) & 1) t = T_HIT;
+        if (bx) r.kx -= 1;
+        if (by) r.ky -= 1;
+        if (bz) r.kz -= 1;
+        const bool out = (r.kx | r.ky | r.kz) < 0;
+        bool hb = false;
+        if (r.m) {
+            if (bx) r.bi += r.sx;
+            if (by) r.bi += 4 * r.sy;
+            if (bz) r.bi += 16 * r.sz;
+            hb = !out && ((r.m >> (r.bi & 63)) & 1);
         }
-        if (t != T_LIVE) {
-            result = t;
-            axis = bx ? 0 : (by ? 1 : 2);
-            cd = bx ? r.tx : (by ? r.ty : r.tz);
-            sgn = bx ? r.sx : (by ? r.sy : r.sz);
-            break;
+        if (out | hb | (r.left == 0)) {
+            const int a = bx ? 0 : (by ? 1 : 2);
+            if (out) {
+                refills++;
+                const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
+                const int t = enter_box<SMEM>(r, cx, cy, cz, P, rdist, bb, exact);
+                if (t == T_HIT) { result = T_HIT; hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz; }
+                else if (t == T_MISS) result = T_MISS;
+                else result = T_LIVE;
+            } else if (hb) {
+                result = T_HIT;
+                const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
+                hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz;
+            } else {
+                result = T_MISS;  // the step cap: this was the last iteration
+            }
+            if (result != T_LIVE) {
+                axis = a;
+                cd = a == 0 ? r.tx : (a == 1 ? r.ty : r.tz);
+                sgn = a == 0 ? r.sx : (a == 1 ? r.sy : r.sz);
+                break;
+            }
+            if (r.left == 0) { result = T_MISS; break; }  // entered an empty box on the last iteration
         }
         if (bx) r.tx = fadd(r.tx, r.dx);
         if (by) r.ty = fadd(r.ty, r.dy);
         if (bz) r.tz = fadd(r.tz, r.dz);
+        r.left -= 1;
     }
-    steps += n0 - r.rem;
-    if (result == T_HIT) hit_index = r.cx + P.L.W * r.cy + P.L.W * P.L.H * r.cz;
+    steps += n0 - r.left;  // r.left counts down from n0-1 and the breaking step was not subtracted
     return result;
 }
 
+__device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
+    if (P.nviews == 1) return 0;
+    int lo = 0, hi = P.nviews - 1;
+    while (lo < hi) {  // the last view whose first tile is <= t
+        const int mid = (lo + hi + 1) >> 1;
+        if (P.views[mid].tile_begin <= t) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// One CTA per ray tile (tile_w x tile_h pixels, tile_w*tile_h == blockDim.x) over the tile
+// space of every view of the launch: a single frame, or a batch of cameras of any sizes.
 template <bool SMEM>
-__global__ void __launch_bounds__(128) render_mask_pixel_kernel(const __grid_constant__ MaskParams P) {
+__global__ void __launch_bounds__(128) render_tiles_kernel(const __grid_constant__ MaskParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     const uint8_t* rdist = P.rdist;
     if (SMEM) {
@@ -631,9 +743,11 @@ __global__ void __launch_bounds__(128) render_mask_pixel_kernel(const __grid_con
         __syncthreads();
         rdist = smem;
     }
-    const ViewDev& V = P.v0;
-    const int px = blockIdx.x * 16 + (threadIdx.x & 15);
-    const int py = blockIdx.y * 8 + (threadIdx.x >> 4);
+    const int tile = blockIdx.x;
+    const ViewDev& V = view_of(P, view_of_tile(P, tile));
+    const int lt = tile - V.tile_begin;
+    const int px = (lt % V.tiles_x) * V.tile_w + (int)threadIdx.x % V.tile_w;
+    const int py = (lt / V.tiles_x) * V.tile_h + (int)threadIdx.x / V.tile_w;
     const bool valid = px < V.width && py < V.height;
     PixelResult res{};
     unsigned refills = 0;
@@ -641,10 +755,13 @@ __global__ void __launch_bounds__(128) render_mask_pixel_kernel(const __grid_con
         const vrt_uniforms& u = V.u;
         const V3 cam{u.camPos[0], u.camPos[1], u.camPos[2]};
         const V3 rd = primary_dir(u, px, py, V.width, V.height);
-        float cd = 0.f;
-        int axis = 2, sgn = 0, steps = 0;
+        float cd = 0.f, c2;
+        int axis = 2, sgn = 0, steps = 0, a2, s2;
         int32_t hit = -1, dummy = -1;
-        const int pr = cast_mask<SMEM>(P, rdist, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit, refills);
+        const int* bb = P.aabb;  // read at box lookups only
+        const bool exact = V.exact != 0;
+        const int pr = cast_box<SMEM>(P, rdist, bb, exact, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit,
+                                      refills);
         res.primary_steps = steps;
         float mr = u.ambient, mg = u.ambient, mb = u.ambient;
         int32_t word = 0;
@@ -654,10 +771,8 @@ __global__ void __launch_bounds__(128) render_mask_pixel_kernel(const __grid_con
             const V3 hp = add3(mul3s(rd, cd), cam);
             const V3 hn = axis_normal(axis, sgn);
             const V3 toLight = norm3(sub3(V3{u.lightPos[0], u.lightPos[1], u.lightPos[2]}, hp));
-            float c2;
-            int a2, s2;
-            const int sr = cast_mask<SMEM>(P, rdist, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
-                                           u.maxSteps, c2, a2, s2, steps, dummy, refills);
+            const int sr = cast_box<SMEM>(P, rdist, bb, exact, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
+                                          u.maxSteps, c2, a2, s2, steps, dummy, refills);
             res.cast |= 1u;
             if (sr != T_HIT) {
                 const float c = fmul(u.diffuse, fmax0(dot3(hn, toLight)));
@@ -675,8 +790,9 @@ __global__ void __launch_bounds__(128) render_mask_pixel_kernel(const __grid_con
                     const float ld = len3(sub3(Lp, hp));
                     if (ld <= R) {
                         const V3 tl = norm3(sub3(Lp, hp));
-                        const int lr = cast_mask<SMEM>(P, rdist, add3(hp, mul3s(tl, 0.001f)), tl, f2i(fadd(ld, 1.0f)),
-                                                       u.maxSteps, c2, a2, s2, steps, dummy, refills);
+                        const int lr = cast_box<SMEM>(P, rdist, bb, exact, add3(hp, mul3s(tl, 0.001f)), tl,
+                                                      f2i(fadd(ld, 1.0f)), u.maxSteps, c2, a2, s2, steps, dummy,
+                                                      refills);
                         res.cast |= 2u << i;
                         if (lr != T_HIT) {
                             const float nl = fmax0(dot3(hn, tl));
@@ -768,18 +884,35 @@ static int check_uniforms(const vrt_uniforms* u) {
 }
 
 struct Tuning {
-    int tile_w, tile_h, refill_min, blocks_per_sm;
+    int tile_w, tile_h, refill_min, blocks_per_sm, exact_steps;
 };
 
 static Tuning tuning_of(const vrt_render_opts* o) {
-    Tuning t{8, 4, 8, 4};
+    Tuning t{8, 4, 8, 4, 0};
     if (o) {
+        t.exact_steps = o->exact_steps != 0;
         if (o->tile_w > 0) t.tile_w = o->tile_w;
         if (o->tile_h > 0) t.tile_h = o->tile_h;
         if (o->refill_min > 0) t.refill_min = std::min(o->refill_min, 32);
         if (o->blocks_per_sm > 0) t.blocks_per_sm = std::min(o->blocks_per_sm, 8);
     }
     return t;
+}
+
+// Ray tiles of the tile kernel: one CTA each, tile_w * tile_h threads (a multiple of 32,
+// at most 128); 8x16 unless the options name another shape (the fastest of 8x4 ... 128x1
+// on the 1080p frame; 8x8 ties).
+static int tile_tuning(const vrt_render_opts* o, Tuning* t) {
+    *t = tuning_of(o);
+    if (!o || o->tile_w <= 0 || o->tile_h <= 0) {
+        t->tile_w = 8;
+        t->tile_h = 16;
+    }
+    const int n = t->tile_w * t->tile_h;
+    if (n % 32 != 0 || n > 128)
+        return set_error(VRT_EINVAL, "ray tile %dx%d: tile_w*tile_h must be a multiple of 32 up to 128", t->tile_w,
+                         t->tile_h);
+    return VRT_OK;
 }
 
 // Region distances go to shared memory when they take at most this many bytes
@@ -794,6 +927,7 @@ static int launch_mask(vrt_renderer* r, const vrt_world* w, const ViewDev* h_vie
     P.bricks = w->d_bricks;
     P.bdist = w->d_bdist;
     P.rdist = w->d_rdist;
+    P.aabb = w->d_aabb;
     P.L = w->L;
     P.views = nviews == 1 ? nullptr : d_views;
     P.nviews = nviews;
@@ -819,24 +953,26 @@ static int launch_mask(vrt_renderer* r, const vrt_world* w, const ViewDev* h_vie
     return VRT_OK;
 }
 
-static int launch_mask_pixel(const vrt_world* w, const ViewDev& v, cudaStream_t s) {
+// Tile kernel launch over the views' tile space (1 view: h_views[0] as a parameter).
+static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, int total_tiles,
+                        const ViewDev* d_views, int threads, cudaStream_t s) {
     MaskParams P;
     std::memset(&P, 0, sizeof(P));
     P.words = w->d_words;
     P.bricks = w->d_bricks;
     P.bdist = w->d_bdist;
     P.rdist = w->d_rdist;
+    P.aabb = w->d_aabb;
     P.L = w->L;
-    P.nviews = 1;
-    P.v0 = v;
+    P.views = nviews == 1 ? nullptr : d_views;
+    P.nviews = nviews;
+    P.total_tiles = total_tiles;
+    P.v0 = h_views[0];
     const int region_bytes = w->L.RWp * w->L.RHp * w->L.RWp;
     P.region_bytes16 = (region_bytes + 15) & ~15;
-    const bool smem_regions = P.region_bytes16 <= kSmemRegionLimit;
-    const size_t smem = smem_regions ? P.region_bytes16 : 0;
-    auto kern = smem_regions ? render_mask_pixel_kernel<true> : render_mask_pixel_kernel<false>;
-    VRT_CUDA(cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    dim3 grid((v.width + 15) / 16, (v.height + 7) / 8);
-    kern<<<grid, 128, smem, s>>>(P);
+    // region distances are read through L1 (staging them per CTA costs more than it saves)
+    auto kern = render_tiles_kernel<false>;
+    if (total_tiles > 0) kern<<<total_tiles, threads, 0, s>>>(P);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
@@ -855,6 +991,7 @@ static void fill_view(ViewDev& v, const vrt_uniforms& u, int width, int height, 
     v.rgba = rgba;
     if (dbg) v.dbg = *dbg;
     v.stats = reinterpret_cast<unsigned long long*>(stats);
+    v.exact = t.exact_steps || u.viewDepthField == 1 || (dbg && (dbg->steps || dbg->primary_steps));
 }
 
 static inline int tiles_of(int width, int height, const Tuning& t) {
@@ -928,10 +1065,12 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
     if (kernel == VRT_KERNEL_MASK_PIXEL) {
         if (w->has_depth_field)
             return set_error(VRT_ESTATE, "the world holds depth-field words, which only the word kernel follows");
-        Tuning t = tuning_of(opts);
+        Tuning t;
+        int st = tile_tuning(opts, &t);
+        if (st) return st;
         ViewDev v;
         fill_view(v, *u, width, height, d_rgba, dbg, d_stats, t, 0);
-        return launch_mask_pixel(w, v, S(stream));
+        return launch_tiles(w, &v, 1, tiles_of(width, height, t), nullptr, t.tile_w * t.tile_h, S(stream));
     }
     if (kernel != VRT_KERNEL_BITMASK) return set_error(VRT_EINVAL, "unknown kernel %d", kernel);
     Tuning t = tuning_of(opts);
@@ -984,14 +1123,37 @@ static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, st
     return VRT_OK;
 }
 
+// Batches run the tile kernel (AUTO, MASK_PIXEL) or the persistent kernel (BITMASK).
+static int batch_tuning(const vrt_render_opts* opts, Tuning* t, bool* tiles) {
+    const int kernel = opts ? opts->kernel : VRT_KERNEL_AUTO;
+    if (kernel == VRT_KERNEL_BITMASK) {
+        *tiles = false;
+        *t = tuning_of(opts);
+        return VRT_OK;
+    }
+    if (kernel != VRT_KERNEL_AUTO && kernel != VRT_KERNEL_MASK_PIXEL)
+        return set_error(VRT_EINVAL, "batches render with the occupancy-mask kernels, not kernel %d", kernel);
+    *tiles = true;
+    return tile_tuning(opts, t);
+}
+
+static int launch_batch(vrt_renderer* r, const vrt_world* w, const std::vector<ViewDev>& hv, int total,
+                        const Tuning& t, bool tiles, const ViewDev* d_views, unsigned* d_counter, cudaStream_t s) {
+    if (tiles) return launch_tiles(w, hv.data(), (int)hv.size(), total, d_views, t.tile_w * t.tile_h, s);
+    return launch_mask(r, w, hv.data(), (int)hv.size(), total, t, d_views, d_counter, s);
+}
+
 int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count, const vrt_render_opts* opts,
                      void* stream) {
     if (!r) return set_error(VRT_EINVAL, "NULL renderer");
-    Tuning t = tuning_of(opts);
+    Tuning t;
+    bool tiles = true;
+    int st = batch_tuning(opts, &t, &tiles);
+    if (st) return st;
     std::vector<ViewDev> hv;
     const vrt_world* w = nullptr;
     int total = 0;
-    int st = build_batch(views, count, t, hv, &w, &total);
+    st = build_batch(views, count, t, hv, &w, &total);
     if (st) return st;
     if (count > 1) {
         st = ensure_views(r, count);
@@ -999,18 +1161,21 @@ int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count, cons
         // pageable source: the copy is staged before the call returns, so hv may go
         VRT_CUDA(cudaMemcpyAsync(r->d_views, hv.data(), sizeof(ViewDev) * count, cudaMemcpyHostToDevice, S(stream)));
     }
-    return launch_mask(r, w, hv.data(), count, total, t, r->d_views, r->d_counter, S(stream));
+    return launch_batch(r, w, hv, total, t, tiles, r->d_views, r->d_counter, S(stream));
 }
 
 int vrt_batch_graph_create(vrt_renderer* r, const vrt_view* views, int32_t count, const vrt_render_opts* opts,
                            void* stream, vrt_batch_graph** out) {
     if (!r || !out) return set_error(VRT_EINVAL, "NULL argument");
     *out = nullptr;
-    Tuning t = tuning_of(opts);
+    Tuning t;
+    bool tiles = true;
+    int st = batch_tuning(opts, &t, &tiles);
+    if (st) return st;
     std::vector<ViewDev> hv;
     const vrt_world* w = nullptr;
     int total = 0;
-    int st = build_batch(views, count, t, hv, &w, &total);
+    st = build_batch(views, count, t, hv, &w, &total);
     if (st) return st;
     vrt_batch_graph* g = new vrt_batch_graph();
     cudaError_t e = cudaMalloc(&g->d_views, sizeof(ViewDev) * (size_t)count);
@@ -1028,7 +1193,7 @@ int vrt_batch_graph_create(vrt_renderer* r, const vrt_view* views, int32_t count
         vrt_batch_graph_destroy(g);
         return cuda_error(e, "cudaStreamBeginCapture");
     }
-    st = launch_mask(r, w, hv.data(), count, total, t, g->d_views, g->d_counter, g->capture_stream);
+    st = launch_batch(r, w, hv, total, t, tiles, g->d_views, g->d_counter, g->capture_stream);
     e = cudaStreamEndCapture(g->capture_stream, &g->graph);
     if (st || e != cudaSuccess) {
         vrt_batch_graph_destroy(g);

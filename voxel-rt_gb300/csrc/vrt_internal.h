@@ -81,6 +81,8 @@ struct vrt_world {
     uint8_t* d_tmp_a = nullptr;     // scratch of the distance passes (n_bricks each)
     uint8_t* d_tmp_b = nullptr;
     int* d_flag = nullptr;          // has-depth-field flag written by the mask kernels
+    int* d_aabb = nullptr;          // bounding box of the solid voxels, brick-granular and
+                                    // never smaller than the truth: min x,y,z then max x,y,z
     int has_depth_field = 0;        // host copy (as of the last sync)
     uint64_t device_bytes = 0;
     int device = 0;

@@ -8,6 +8,7 @@
 #include <cuda_runtime.h>
 
 #include <algorithm>
+#include <climits>
 #include <cmath>
 #include <cstring>
 #include <mutex>
@@ -41,7 +42,7 @@ Layout make_layout(int W, int H) {
 // One thread per brick of the brick box [b0, b1): OR of (word >= 0) over its 4x4x4
 // voxels; any word < -1 raises the depth-field flag.
 __global__ void brick_mask_kernel(const int32_t* __restrict__ words, uint64_t* __restrict__ bricks, int* flag,
-                                  Layout L, int bx0, int by0, int bz0, int nbx, int nby, int nbz) {
+                                  int* aabb, Layout L, int bx0, int by0, int bz0, int nbx, int nby, int nbz) {
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     uint64_t total = (uint64_t)nbx * nby * nbz;
     if (t >= total) return;
@@ -74,6 +75,27 @@ __global__ void brick_mask_kernel(const int32_t* __restrict__ words, uint64_t* _
     }
     bricks[brick_index(L, bx, by, bz)] = m;
     if (depth) atomicOr(flag, 1);
+    // grow the solid bounding box by this brick (one atomic per warp and bound)
+    const unsigned mask = __activemask();
+    int v[6];
+    if (m) {
+        v[0] = 4 * bx; v[1] = 4 * by; v[2] = 4 * bz;
+        v[3] = 4 * bx + 3; v[4] = 4 * by + 3; v[5] = 4 * bz + 3;
+    } else {
+        v[0] = v[1] = v[2] = INT_MAX;
+        v[3] = v[4] = v[5] = INT_MIN;
+    }
+    for (int i = 0; i < 3; i++) v[i] = __reduce_min_sync(mask, v[i]);
+    for (int i = 3; i < 6; i++) v[i] = __reduce_max_sync(mask, v[i]);
+    if ((threadIdx.x & 31) == (__ffs(mask) - 1) && v[0] != INT_MAX) {
+        for (int i = 0; i < 3; i++) atomicMin(aabb + i, v[i]);
+        for (int i = 3; i < 6; i++) atomicMax(aabb + i, v[i]);
+    }
+}
+
+__global__ void reset_aabb_kernel(int* aabb) {
+    if (threadIdx.x < 3) aabb[threadIdx.x] = INT_MAX;
+    else if (threadIdx.x < 6) aabb[threadIdx.x] = INT_MIN;
 }
 
 // One thread per node of the parent box: bit i set when child i is non-zero.
@@ -173,8 +195,10 @@ int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int 
     int bx0 = x0 >> 2, by0 = y0 >> 2, bz0 = z0 >> 2;
     int bx1 = (x1 + 3) >> 2, by1 = (y1 + 3) >> 2, bz1 = (z1 + 3) >> 2;
     uint64_t nb = (uint64_t)(bx1 - bx0) * (by1 - by0) * (bz1 - bz0);
-    brick_mask_kernel<<<blocks_for(nb, 256), 256, 0, s>>>(w->d_words, w->d_bricks, w->d_flag, L, bx0, by0, bz0,
-                                                           bx1 - bx0, by1 - by0, bz1 - bz0);
+    // a refresh of the whole world recomputes the solid bounding box; a partial one only grows it
+    if (x0 == 0 && y0 == 0 && z0 == 0 && x1 == L.W && y1 == L.H && z1 == L.W) reset_aabb_kernel<<<1, 32, 0, s>>>(w->d_aabb);
+    brick_mask_kernel<<<blocks_for(nb, 256), 256, 0, s>>>(w->d_words, w->d_bricks, w->d_flag, w->d_aabb, L, bx0, by0,
+                                                           bz0, bx1 - bx0, by1 - by0, bz1 - bz0);
     int rx0 = bx0 >> 2, ry0 = by0 >> 2, rz0 = bz0 >> 2;
     int rx1 = (bx1 + 3) >> 2, ry1 = (by1 + 3) >> 2, rz1 = (bz1 + 3) >> 2;
     uint64_t nr = (uint64_t)(rx1 - rx0) * (ry1 - ry0) * (rz1 - rz0);
@@ -386,6 +410,7 @@ int vrt_world_create(int32_t width, int32_t height, vrt_world** out) {
     if (e == cudaSuccess) e = cudaMalloc(&w->d_tmp_a, w->L.n_bricks);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_tmp_b, w->L.n_bricks);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_flag, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_aabb, 8 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(w->d_words, 0xFF, w->L.n_words * 4);  // air = -1 (render.cpp:349-351)
     if (e == cudaSuccess) e = cudaMemset(w->d_bricks, 0, w->L.n_bricks * 8);
     if (e == cudaSuccess) e = cudaMemset(w->d_regions, 0, w->L.n_regions * 8);
@@ -393,6 +418,10 @@ int vrt_world_create(int32_t width, int32_t height, vrt_world** out) {
     if (e == cudaSuccess) e = cudaMemset(w->d_bdist, kDistCap, w->L.n_bricks);  // an all-air world
     if (e == cudaSuccess) e = cudaMemset(w->d_rdist, kDistCap, rbytes);
     if (e == cudaSuccess) e = cudaMemset(w->d_flag, 0, sizeof(int));
+    if (e == cudaSuccess) {  // an all-air world: empty box (min > max)
+        const int empty[8] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, 0, 0};
+        e = cudaMemcpy(w->d_aabb, empty, sizeof(empty), cudaMemcpyHostToDevice);
+    }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
         cudaGetLastError();
@@ -416,6 +445,7 @@ int vrt_world_destroy(vrt_world* w) {
     cudaFree(w->d_tmp_a);
     cudaFree(w->d_tmp_b);
     cudaFree(w->d_flag);
+    cudaFree(w->d_aabb);
     delete w;
     return VRT_OK;
 }

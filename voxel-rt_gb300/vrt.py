@@ -77,6 +77,7 @@ class RenderOpts(C.Structure):
         ("tile_h", C.c_int32),
         ("refill_min", C.c_int32),
         ("blocks_per_sm", C.c_int32),
+        ("exact_steps", C.c_int32),
     ]
 
 
