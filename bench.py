@@ -394,8 +394,8 @@ def bench_served(vrt, torch, scenes, sc, full_world):
     srv = serving.Server(40 << 30, slots=4, max_batch=8)
     wids = [srv.add_world(s.world) for s in specs]
     results = []
-    for rate in (50.0, 200.0, 800.0):
-        reqs = serving.make_requests(specs, rate, 1.5, seed=int(rate))
+    for rate in (250.0, 1000.0, 4000.0, 16000.0):
+        reqs = serving.make_requests(specs, rate, 1.0, seed=int(rate))
         done, wall = serving.run_open_loop(srv, wids, reqs)
         res = serving.summarize(done, wall)
         res["rate_hz"] = rate

@@ -115,7 +115,7 @@ typedef struct vrt_render_opts {
     int32_t kernel;          /* VRT_KERNEL_*                                        */
     int32_t tile_w, tile_h;  /* ray tile (0 = kernel default: 8x16 tile kernel, 8x4 persistent) */
     int32_t refill_min;      /* persistent kernel: lanes parked before a slow phase (0 = default) */
-    int32_t blocks_per_sm;   /* persistent kernel: resident CTAs per SM (0 = default) */
+    int32_t blocks_per_sm;   /* resident CTAs per SM the kernel is built for (persistent: 3-4, tile: 8, 10, 12) */
     int32_t exact_steps;     /* 1: count every DDA iteration of the shader, no early miss */
 } vrt_render_opts;
 
@@ -187,9 +187,10 @@ int vrt_fix_depth_field_box(vrt_world* w, int32_t x0, int32_t y0, int32_t z0,
 
 /* ---- world generation ---- */
 /* initVoxels, level.cpp:82-138 (stone/dirt/grass layers and trees, including the
- * reference's relative-coordinate destroyVoxel calls), run on the device.  The world
- * must be 512 x 96 x 512, the size level.cpp is written for.  Depth field not included:
- * call vrt_fix_depth_field_box over the whole world for the app's init state. */
+ * reference's relative-coordinate destroyVoxel calls), run on the device; level.cpp is
+ * written for 512 x 96 x 512, other sizes run the same rules.  Synchronises the stream.
+ * Depth field not included: call vrt_fix_depth_field_box over the whole world for the
+ * app's init state. */
 int vrt_world_init_reference(vrt_world* w, void* stream);
 /* Seeded terrain of the benchmark scenes (host, multi-threaded, deterministic across
  * CPUs): 2-octave value-noise heightfield in [8,40], grass/dirt/stone bands with +-8

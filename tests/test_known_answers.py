@@ -192,3 +192,16 @@ def test_kernels_on_known_answer_scenes(cuda, oracle, kernel):
             assert_same_frame(o, g)
         except AssertionError as e:
             raise AssertionError(f"scene {name}: {e}") from None
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("kernel", [vrt.KERNEL_BITMASK, vrt.KERNEL_MASK_PIXEL])
+def test_fast_mode_on_known_answer_scenes(cuda, oracle, kernel):
+    """Images only (rays that cannot hit may end early): still the oracle's pixels."""
+    for name, words, u, width, height in kat_scenes():
+        if u.viewDepthField == 1:
+            continue  # the step view always counts exactly
+        o = oracle.render(words, S, S, u, width, height)
+        g = gpu_render(make_world(words, S, S), u, width, height, kernel=kernel, debug=False)
+        assert np.array_equal(o["rgba"], g["rgba"]), f"scene {name}"
+        assert int(g["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"], f"scene {name}"

@@ -191,7 +191,7 @@ struct MaskParams {
     const uint64_t* bricks;
     const uint8_t* bdist;
     const uint8_t* rdist;
-    const int* aabb;       // solid bounding box: min x,y,z, max x,y,z (never smaller than the truth)
+    int bb[6];             // solid bounding box: min x,y,z, max x,y,z (never smaller than the truth)
     Layout L;
     const ViewDev* views;  // nviews entries (device); NULL when nviews == 1 (v0 is used)
     int nviews;
@@ -249,19 +249,19 @@ __device__ __forceinline__ int start_ray(Ray& r, V3 o, V3 d, int n, int maxSteps
 // A ray in cell c cannot hit anything if, along some axis, c lies beyond the solid
 // bounding box and the ray moves away from it or parallel to it: every later cell stays
 // beyond the box along that axis.
-__device__ __forceinline__ bool beyond_solids(const int* bb, int cx, int cy, int cz, int sx, int sy, int sz) {
-    return (cx < __ldg(bb + 0) && sx <= 0) || (cy < __ldg(bb + 1) && sy <= 0) || (cz < __ldg(bb + 2) && sz <= 0) ||
-           (cx > __ldg(bb + 3) && sx >= 0) || (cy > __ldg(bb + 4) && sy >= 0) || (cz > __ldg(bb + 5) && sz >= 0);
+__device__ __forceinline__ bool beyond_solids(const MaskParams& P, int cx, int cy, int cz, int sx, int sy, int sz) {
+    return (cx < P.bb[0] && sx <= 0) || (cy < P.bb[1] && sy <= 0) || (cz < P.bb[2] && sz <= 0) ||
+           (cx > P.bb[3] && sx >= 0) || (cy > P.bb[4] && sy >= 0) || (cz > P.bb[5] && sz >= 0);
 }
 
 // The parked step moved the ray into cell c outside its box: bound the largest known
 // box around c from the distance fields, or load the brick's voxel bits.
 template <bool SMEM>
-__device__ __forceinline__ int refill(Ray& r, const MaskParams& P, const uint8_t* rdist, const int* bb, bool exact) {
+__device__ __forceinline__ int refill(Ray& r, const MaskParams& P, const uint8_t* rdist, bool exact) {
     const Layout& L = P.L;
     if ((unsigned)r.cx >= (unsigned)L.W || (unsigned)r.cy >= (unsigned)L.H || (unsigned)r.cz >= (unsigned)L.W)
         return T_MISS;  // getVoxelIndex == -1 (fshader.glsl:123-125)
-    if (!exact && beyond_solids(bb, r.cx, r.cy, r.cz, r.sx, r.sy, r.sz)) return T_MISS;
+    if (!exact && beyond_solids(P, r.cx, r.cy, r.cz, r.sx, r.sy, r.sz)) return T_MISS;
     const int rx = r.cx >> 4, ry = r.cy >> 4, rz = r.cz >> 4;
     const uint64_t rl = region_linear(L, rx, ry, rz);
     const int dr = SMEM ? (int)rdist[rl] : (int)__ldg(rdist + rl);
@@ -329,7 +329,7 @@ __global__ void __launch_bounds__(kThreads, MINB) render_mask_kernel(const __gri
         n_slow++;
         if (mode == M_BOX) {
             LSU(F_ST_REFILLS) += 1u;
-            const int t = refill<SMEM>(r, P, rdist, P.aabb, view_of(P, (int)LSU(F_VID)).exact != 0);
+            const int t = refill<SMEM>(r, P, rdist, view_of(P, (int)LSU(F_VID)).exact != 0);
             if (t == T_LIVE) {
                 if (r.la == 0) r.tx = fadd(r.tx, r.dx);
                 else if (r.la == 1) r.ty = fadd(r.ty, r.dy);
@@ -605,9 +605,8 @@ struct BoxRay {
 };
 
 __device__ __forceinline__ void set_axis(int c, int s, int lo, int hi, int& k, int& e) {
-    if (s > 0) { k = hi - 1 - c; e = hi; }
-    else if (s < 0) { k = c - lo; e = lo - 1; }
-    else { k = INT_MAX; e = c; }
+    k = s > 0 ? hi - 1 - c : (s < 0 ? c - lo : INT_MAX);
+    e = s > 0 ? hi : (s < 0 ? lo - 1 : c);
 }
 
 // The ray stands in cell c, outside any known box: bound the largest empty box around
@@ -615,11 +614,11 @@ __device__ __forceinline__ void set_axis(int c, int s, int lo, int hi, int& k, i
 // T_MISS (c is outside the world).
 template <bool SMEM>
 __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, const MaskParams& P,
-                                         const uint8_t* rdist, const int* bb, bool exact) {
+                                         const uint8_t* rdist, bool exact) {
     const Layout& L = P.L;
     if ((unsigned)cx >= (unsigned)L.W || (unsigned)cy >= (unsigned)L.H || (unsigned)cz >= (unsigned)L.W)
         return T_MISS;  // getVoxelIndex == -1 (fshader.glsl:123-125)
-    if (!exact && beyond_solids(bb, cx, cy, cz, r.sx, r.sy, r.sz)) return T_MISS;
+    if (!exact && beyond_solids(P, cx, cy, cz, r.sx, r.sy, r.sz)) return T_MISS;
     const int rx = cx >> 4, ry = cy >> 4, rz = cz >> 4;
     const uint64_t rl = region_linear(L, rx, ry, rz);
     const int dr = SMEM ? (int)rdist[rl] : (int)__ldg(rdist + rl);
@@ -653,7 +652,7 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
 // only when the ray leaves its known box.  On a hit, cd / axis / sgn / cell describe the
 // last step (currDist, hitNormal, the voxel).
 template <bool SMEM>
-__device__ __forceinline__ int cast_box(const MaskParams& P, const uint8_t* rdist, const int* bb, bool exact, V3 o,
+__device__ __forceinline__ int cast_box(const MaskParams& P, const uint8_t* rdist, bool exact, V3 o,
                                         V3 d, int n, int maxSteps, float& cd, int& axis, int& sgn, int& steps,
                                         int32_t& hit_index, unsigned& refills) {
     RaySetup s;
@@ -691,7 +690,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const uint8_t* rdis
             if (out) {
                 refills++;
                 const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
-                const int t = enter_box<SMEM>(r, cx, cy, cz, P, rdist, bb, exact);
+                const int t = enter_box<SMEM>(r, cx, cy, cz, P, rdist, exact);
                 if (t == T_HIT) { result = T_HIT; hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz; }
                 else if (t == T_MISS) result = T_MISS;
                 else result = T_LIVE;
@@ -758,9 +757,8 @@ __global__ void __launch_bounds__(128) render_tiles_kernel(const __grid_constant
         float cd = 0.f, c2;
         int axis = 2, sgn = 0, steps = 0, a2, s2;
         int32_t hit = -1, dummy = -1;
-        const int* bb = P.aabb;  // read at box lookups only
         const bool exact = V.exact != 0;
-        const int pr = cast_box<SMEM>(P, rdist, bb, exact, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit,
+        const int pr = cast_box<SMEM>(P, rdist, exact, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit,
                                       refills);
         res.primary_steps = steps;
         float mr = u.ambient, mg = u.ambient, mb = u.ambient;
@@ -771,7 +769,7 @@ __global__ void __launch_bounds__(128) render_tiles_kernel(const __grid_constant
             const V3 hp = add3(mul3s(rd, cd), cam);
             const V3 hn = axis_normal(axis, sgn);
             const V3 toLight = norm3(sub3(V3{u.lightPos[0], u.lightPos[1], u.lightPos[2]}, hp));
-            const int sr = cast_box<SMEM>(P, rdist, bb, exact, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
+            const int sr = cast_box<SMEM>(P, rdist, exact, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
                                           u.maxSteps, c2, a2, s2, steps, dummy, refills);
             res.cast |= 1u;
             if (sr != T_HIT) {
@@ -780,17 +778,22 @@ __global__ void __launch_bounds__(128) render_tiles_kernel(const __grid_constant
             } else {
                 res.occ |= 1u;
             }
+            // R1 = |R|(1 + 2^-10) + 1 exceeds R by more than the rounding of any computed length
             const float ob = u.maxOverbright, R = u.localLightDist;
+            const float R1 = fadd(fmul(fabsf(R), 1.0009765625f), 1.0f);
             for (int i = 0; i < VRT_MAX_LOCAL_LIGHTS; i++) {
                 if (mr >= ob && mg >= ob && mb >= ob) {
                     mr = mg = mb = ob;
                     break;
                 } else if (u.localLights[i][0] >= 0 && u.localLights[i][1] >= 0 && u.localLights[i][2] >= 0) {
                     const V3 Lp{u.localLights[i][0], u.localLights[i][1], u.localLights[i][2]};
-                    const float ld = len3(sub3(Lp, hp));
+                    const V3 dl = sub3(Lp, hp);
+                    // a component beyond R1 puts the computed length beyond R too: out of range
+                    if (fabsf(dl.x) > R1 || fabsf(dl.y) > R1 || fabsf(dl.z) > R1) continue;
+                    const float ld = len3(dl);
                     if (ld <= R) {
-                        const V3 tl = norm3(sub3(Lp, hp));
-                        const int lr = cast_box<SMEM>(P, rdist, bb, exact, add3(hp, mul3s(tl, 0.001f)), tl,
+                        const V3 tl = norm3(dl);
+                        const int lr = cast_box<SMEM>(P, rdist, exact, add3(hp, mul3s(tl, 0.001f)), tl,
                                                       f2i(fadd(ld, 1.0f)), u.maxSteps, c2, a2, s2, steps, dummy,
                                                       refills);
                         res.cast |= 2u << i;
@@ -927,7 +930,7 @@ static int launch_mask(vrt_renderer* r, const vrt_world* w, const ViewDev* h_vie
     P.bricks = w->d_bricks;
     P.bdist = w->d_bdist;
     P.rdist = w->d_rdist;
-    P.aabb = w->d_aabb;
+    std::memcpy(P.bb, w->h_aabb, sizeof(P.bb));
     P.L = w->L;
     P.views = nviews == 1 ? nullptr : d_views;
     P.nviews = nviews;
@@ -962,7 +965,7 @@ static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, 
     P.bricks = w->d_bricks;
     P.bdist = w->d_bdist;
     P.rdist = w->d_rdist;
-    P.aabb = w->d_aabb;
+    std::memcpy(P.bb, w->h_aabb, sizeof(P.bb));
     P.L = w->L;
     P.views = nviews == 1 ? nullptr : d_views;
     P.nviews = nviews;

@@ -83,6 +83,8 @@ struct vrt_world {
     int* d_flag = nullptr;          // has-depth-field flag written by the mask kernels
     int* d_aabb = nullptr;          // bounding box of the solid voxels, brick-granular and
                                     // never smaller than the truth: min x,y,z then max x,y,z
+    int h_aabb[6] = {0, 0, 0, -1, -1, -1};  // host copy passed to the render kernels; kept a
+                                    // superset of the device box (read back after uploads)
     int has_depth_field = 0;        // host copy (as of the last sync)
     uint64_t device_bytes = 0;
     int device = 0;

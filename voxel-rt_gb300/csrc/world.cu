@@ -226,6 +226,16 @@ int refresh_masks(vrt_world* w, uint64_t first, uint64_t count, cudaStream_t s) 
     return refresh_masks_box(w, x0, y0, z0, x1 + 1, y0 + 1, z0 + 1, s);
 }
 
+// Copy the device solid bounding box to the host copy the render launches pass on
+// (synchronises the stream).
+static int read_aabb(vrt_world* w, cudaStream_t s) {
+    int bb[8];
+    VRT_CUDA(cudaMemcpyAsync(bb, w->d_aabb, sizeof(bb), cudaMemcpyDeviceToHost, s));
+    VRT_CUDA(cudaStreamSynchronize(s));
+    for (int i = 0; i < 6; i++) w->h_aabb[i] = bb[i];
+    return VRT_OK;
+}
+
 // ------------------------------------------------------------------ edits
 
 // removeSphere's first loop (level.cpp:31-42): voxels with offsets in [-r,r)^3,
@@ -421,6 +431,7 @@ int vrt_world_create(int32_t width, int32_t height, vrt_world** out) {
     if (e == cudaSuccess) {  // an all-air world: empty box (min > max)
         const int empty[8] = {INT_MAX, INT_MAX, INT_MAX, INT_MIN, INT_MIN, INT_MIN, 0, 0};
         e = cudaMemcpy(w->d_aabb, empty, sizeof(empty), cudaMemcpyHostToDevice);
+        for (int i = 0; i < 6; i++) w->h_aabb[i] = empty[i];
     }
     if (e == cudaSuccess) e = cudaDeviceSynchronize();
     if (e != cudaSuccess) {
@@ -478,7 +489,7 @@ static int upload_common(vrt_world* w, const int32_t* src, uint64_t first, uint6
     VRT_CUDA(cudaMemcpyAsync(&flag, w->d_flag, sizeof(int), cudaMemcpyDeviceToHost, S(stream)));
     VRT_CUDA(cudaStreamSynchronize(S(stream)));
     w->has_depth_field |= flag;
-    return VRT_OK;
+    return read_aabb(w, S(stream));
 }
 
 int vrt_world_upload(vrt_world* w, const int32_t* host_words, uint64_t first, uint64_t count, void* stream) {
@@ -522,7 +533,7 @@ int vrt_world_sync_flags(vrt_world* w, void* stream) {
     VRT_CUDA(cudaMemcpyAsync(&flag, w->d_flag, sizeof(int), cudaMemcpyDeviceToHost, S(stream)));
     VRT_CUDA(cudaStreamSynchronize(S(stream)));
     w->has_depth_field = flag;
-    return VRT_OK;
+    return read_aabb(w, S(stream));
 }
 
 int vrt_place_voxel(vrt_world* w, int32_t x, int32_t y, int32_t z, int32_t word, void* stream) {
@@ -531,6 +542,13 @@ int vrt_place_voxel(vrt_world* w, int32_t x, int32_t y, int32_t z, int32_t word,
     place_voxel_kernel<<<1, 1, 0, S(stream)>>>(w->d_words, w->L, x, y, z, word);
     VRT_CUDA(cudaGetLastError());
     if (word < -1) w->has_depth_field = 1;
+    if (word >= 0) {  // grow the host copy of the solid box by the voxel's brick
+        const int c[3] = {x & ~3, y & ~3, z & ~3};
+        for (int i = 0; i < 3; i++) {
+            w->h_aabb[i] = std::min(w->h_aabb[i], c[i]);
+            w->h_aabb[3 + i] = std::max(w->h_aabb[3 + i], c[i] + 3);
+        }
+    }
     return refresh_masks_box(w, x, y, z, x + 1, y + 1, z + 1, S(stream));
 }
 
@@ -591,7 +609,9 @@ int vrt_world_init_reference(vrt_world* w, void* stream) {
     }
     VRT_CUDA(cudaMemsetAsync(w->d_flag, 0, sizeof(int), S(stream)));
     w->has_depth_field = 0;
-    return refresh_masks_box(w, 0, 0, 0, L.W, L.H, L.W, S(stream));
+    int st = refresh_masks_box(w, 0, 0, 0, L.W, L.H, L.W, S(stream));
+    if (st) return st;
+    return read_aabb(w, S(stream));
 }
 
 }  // extern "C"
