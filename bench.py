@@ -318,6 +318,7 @@ def main():
         line["batched"] = bench_batched(vrt, torch, scenes, sc, world, r, dev, stream)
         line["served"] = bench_served(vrt, torch, scenes, sc, world)
         line["served"]["plain_frame_ms"] = ms
+        line["stress"] = bench_stress(vrt, torch, scenes, dev, stream)
         line["cpu_baseline"] = cpu_baseline(sc, args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line), flush=True)
@@ -333,27 +334,29 @@ def C_sizeof_uniforms():
 
 
 def bench_batched(vrt, torch, scenes, sc, world, r, dev, stream):
-    """64 cameras in one graph-captured persistent launch vs one launch per camera."""
+    """64 cameras: one CUDA-graph-captured launch with autotuned ray tiles per resolution
+    class, against one vrt_render launch per camera."""
     import ctypes as C
+    import autotune
     views = scenes.batch_views(sc, 64, seed=3)
     imgs = [torch.empty(w * h * 4, dtype=torch.uint8, device=dev) for (_, w, h) in views]
+    ptrs = [im.data_ptr() for im in imgs]
     stats = torch.zeros((len(views), vrt.STAT_COUNT), dtype=torch.int64, device=dev)
-    vv = [vrt.make_view(world, u, w, h, im.data_ptr(), stats[i].data_ptr())
-          for i, ((u, w, h), im) in enumerate(zip(views, imgs))]
     sh = stream.cuda_stream
-    r.render_batch(vv, None, sh)
+    plan = autotune.tune(torch, r, world, views, ptrs, reps=3)
+    vv = plan.views(world, views, ptrs, [stats[i].data_ptr() for i in range(len(views))])
+    r.render_batch(vv, plan.opts(), sh)
     torch.cuda.synchronize()
     rays = int(stats[:, vrt.STAT_RAYS].sum().item())
-    arr = (vrt.View * len(vv))(*vv)
-    vv_nostats = [vrt.make_view(world, u, w, h, im.data_ptr(), 0) for ((u, w, h), im) in zip(views, imgs)]
-    arr2 = (vrt.View * len(vv_nostats))(*vv_nostats)
+    arr = (vrt.View * len(views))(*plan.views(world, views, ptrs))
     g = C.c_void_p()
-    vrt.check(vrt.lib().vrt_batch_graph_create(r.handle, arr2, len(vv_nostats), None, sh, C.byref(g)))
+    opts = plan.opts()
+    vrt.check(vrt.lib().vrt_batch_graph_create(r.handle, arr, len(views), C.byref(opts), sh, C.byref(g)))
     for _ in range(2):
         vrt.check(vrt.lib().vrt_batch_graph_launch(g, sh))
     torch.cuda.synchronize()
     a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    reps = 3
+    reps = 5
     a.record(stream)
     for _ in range(reps):
         vrt.check(vrt.lib().vrt_batch_graph_launch(g, sh))
@@ -361,21 +364,62 @@ def bench_batched(vrt, torch, scenes, sc, world, r, dev, stream):
     torch.cuda.synchronize()
     batched_ms = a.elapsed_time(b) / reps
     vrt.lib().vrt_batch_graph_destroy(g)
-    # plain: one vrt_render launch per camera
-    for (u, w, h), im in zip(views, imgs):
-        r.render(world, u, w, h, im.data_ptr(), None, 0, None, sh)
+    # plain: one vrt_render launch per camera, default options
+    for (u, w, h), p in zip(views, ptrs):
+        r.render(world, u, w, h, p, None, 0, None, sh)
     torch.cuda.synchronize()
     a.record(stream)
     for _ in range(reps):
-        for (u, w, h), im in zip(views, imgs):
-            r.render(world, u, w, h, im.data_ptr(), None, 0, None, sh)
+        for (u, w, h), p in zip(views, ptrs):
+            r.render(world, u, w, h, p, None, 0, None, sh)
     b.record(stream)
     torch.cuda.synchronize()
     plain_ms = a.elapsed_time(b) / reps
+    top = sorted(plan.table, key=lambda e: e["ms"])[:4]
     return {"cameras": len(views), "pixels": sum(w * h for _, w, h in views), "rays": rays,
             "batched_ms": batched_ms, "batched_mrays_per_s": rays / (batched_ms * 1e-3) / 1e6,
             "plain_ms": plain_ms, "plain_mrays_per_s": rays / (plain_ms * 1e-3) / 1e6,
-            "speedup": plain_ms / batched_ms}
+            "speedup": plain_ms / batched_ms, "autotuned": plan.describe(), "autotune_best": top}
+
+
+def bench_stress(vrt, torch, scenes, dev, stream):
+    """2048x256x2048 world (4 GiB of words), 3840x2160, 16 local lights + global light,
+    4096 steps, camera 1 voxel above the terrain at pitch -2 deg (grazing rays)."""
+    st = scenes.stress(5, threads=os.cpu_count() or 1)
+    world = vrt.World(st.W, st.H)
+    world.upload(st.words)
+    st.words = None
+    r = vrt.Renderer()
+    W, H = st.width, st.height
+    img = torch.empty(W * H * 4, dtype=torch.uint8, device=dev)
+    stats = torch.zeros(vrt.STAT_COUNT, dtype=torch.int64, device=dev)
+    sh = stream.cuda_stream
+    exact = vrt.RenderOpts()
+    exact.exact_steps = 1
+    r.render(world, st.uniforms, W, H, img.data_ptr(), None, stats.data_ptr(), exact, sh)
+    torch.cuda.synchronize()
+    s_exact = stats.cpu().tolist()
+    stats.zero_()
+    r.render(world, st.uniforms, W, H, img.data_ptr(), None, stats.data_ptr(), None, sh)
+    torch.cuda.synchronize()
+    s_fast = stats.cpu().tolist()
+    flush = torch.empty(256 << 20, dtype=torch.uint8, device=dev)
+    times = []
+    for i in range(5):
+        flush.zero_()
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        r.render(world, st.uniforms, W, H, img.data_ptr(), None, 0, None, sh)
+        b.record(stream)
+        torch.cuda.synchronize()
+        times.append(a.elapsed_time(b))
+    ms = sorted(times)[2]
+    rays = int(s_exact[0])
+    res = {"workload": st.workload, "ms": ms, "mrays_per_s": rays / (ms * 1e-3) / 1e6, "rays": rays,
+           "dda_steps": int(s_exact[1]), "dda_steps_performed": int(s_fast[1]), "box_lookups": int(s_fast[4]),
+           "effective_gbs": (4 * s_exact[1] + 4 * s_exact[2] + 4 * s_exact[3]) / (ms * 1e-3) / 1e9}
+    world.close()
+    return res
 
 
 def bench_served(vrt, torch, scenes, sc, full_world):

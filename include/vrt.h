@@ -168,6 +168,16 @@ int vrt_world_download(const vrt_world* w, int32_t* host_words, uint64_t first, 
  * SH = ceil(H/64); layout as in vrt_world_info.  Synchronises the stream. */
 int vrt_world_download_masks(const vrt_world* w, uint64_t* bricks, uint64_t* regions, uint64_t* supers,
                              void* stream);
+/* Batched voxel lookups, the query behind the reference's collision and gravity probes
+ * (controls.cpp:10-19, :77-98, which read voxels[getVoxelIndex(x,y,z)]): for each of the n
+ * device (x,y,z) int32 triples in d_xyz, d_words[i] = the voxel word, or -1 (air) for a
+ * cell outside the world (the reference reads voxels[-1] there). */
+int vrt_world_probe(const vrt_world* w, const int32_t* d_xyz, int32_t n, int32_t* d_words, void* stream);
+/* World file: a 16-byte header ("VRTW", version 1, W, H as little-endian int32) followed by
+ * the W*H*W voxel words in the reference's in-memory order (x + W*y + W*H*z).  Save
+ * synchronises the stream; load creates the world on the current device. */
+int vrt_world_save(const vrt_world* w, const char* path, void* stream);
+int vrt_world_load(const char* path, vrt_world** out, void* stream);
 /* Recompute has_depth_field (a device reduction; synchronises the stream). */
 int vrt_world_sync_flags(vrt_world* w, void* stream);
 
@@ -225,6 +235,8 @@ typedef struct vrt_view {
     int32_t width, height;
     uint8_t* d_rgba;        /* width*height*4 device bytes */
     uint64_t* d_stats;      /* optional, as vrt_render     */
+    int32_t tile_w, tile_h; /* this view's ray tile in the tile kernel (0 = the launch's);
+                               tile_w*tile_h must equal the launch's tile size */
 } vrt_view;
 
 /* Many cameras (uneven sizes, possibly different worlds without depth fields) in one

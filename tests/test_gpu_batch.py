@@ -83,3 +83,33 @@ def test_batch_rejects_mixed_worlds(cuda, batch_setup):
     vv = [vrt.make_view(w1, views[0][0], 8, 8, img.data_ptr()), vrt.make_view(w2, views[1][0], 8, 8, img.data_ptr())]
     with pytest.raises(vrt.VrtError):
         r.render_batch(vv)
+
+
+def test_per_view_tiles_and_autotuner(cuda, batch_setup):
+    import autotune
+    sc, views = batch_setup
+    w = make_world(sc.words, sc.W, sc.H)
+    r = vrt.Renderer()
+    base, _ = _batch(cuda, r, w, views)
+    imgs = [cuda.zeros(vw * vh * 4, dtype=cuda.uint8, device="cuda") for (_, vw, vh) in views]
+    ptrs = [im.data_ptr() for im in imgs]
+    plan = autotune.tune(cuda, r, w, views, ptrs, reps=1)
+    assert plan.table and plan.describe()["kernel"] in ("tile", "persistent")
+    for im in imgs:
+        im.zero_()
+    r.render_batch(plan.views(w, views, ptrs), plan.opts(), cuda.cuda.current_stream().cuda_stream)
+    cuda.cuda.synchronize()
+    for a, b in zip(base, imgs):
+        assert np.array_equal(a, b.cpu().numpy())
+    # mixed shapes of one thread count in one launch
+    mixed = [vrt.make_view(w, u, vw, vh, p, 0, [(8, 16), (16, 8), (32, 4)][i % 3])
+             for i, ((u, vw, vh), p) in enumerate(zip(views, ptrs))]
+    for im in imgs:
+        im.zero_()
+    r.render_batch(mixed, None, cuda.cuda.current_stream().cuda_stream)
+    cuda.cuda.synchronize()
+    for a, b in zip(base, imgs):
+        assert np.array_equal(a, b.cpu().numpy())
+    bad = [vrt.make_view(w, views[0][0], views[0][1], views[0][2], ptrs[0], 0, (8, 8))]
+    with pytest.raises(vrt.VrtError):
+        r.render_batch(bad, None)  # 64 threads in a 128-thread launch

@@ -83,3 +83,27 @@ def test_partial_upload_refreshes_masks(cuda, vrt_lib):
     # a depth-field word raises the flag, so AUTO renders with the word kernel
     w.upload(np.array([np.float32(-3.0).view(np.int32)], np.int32), 7)
     assert w.info().has_depth_field == 1
+
+
+def test_probe_save_and_load(cuda, vrt_lib, tmp_path):
+    W, H = 64, 64
+    words = vrt_lib.terrain_generate(W, H, 21, 2)
+    w = make_world(words, W, H)
+    rng = np.random.default_rng(2)
+    xyz = np.stack([rng.integers(-3, W + 3, 500), rng.integers(-3, H + 3, 500), rng.integers(-3, W + 3, 500)], 1)
+    xyz = xyz.astype(np.int32)
+    d_xyz = cuda.tensor(xyz.ravel(), device="cuda")
+    d_out = cuda.empty(500, dtype=cuda.int32, device="cuda")
+    w.probe(d_xyz.data_ptr(), 500, d_out.data_ptr())
+    cuda.cuda.synchronize()
+    inside = (xyz >= 0).all(1) & (xyz[:, 0] < W) & (xyz[:, 1] < H) & (xyz[:, 2] < W)
+    want = np.where(inside, words[np.where(inside, xyz[:, 0] + W * xyz[:, 1] + W * H * xyz[:, 2], 0)], -1)
+    assert np.array_equal(d_out.cpu().numpy(), want)
+    path = str(tmp_path / "world.vrtw")
+    w.save(path)
+    w2 = vrt.World.load(path)
+    assert (w2.width, w2.height) == (W, H)
+    assert np.array_equal(w2.download(np.empty_like(words)), words)
+    check_masks(w2, words)
+    raw = np.fromfile(path, dtype=np.int32)
+    assert list(raw[:4]) == [0x57525456, 1, W, H] and np.array_equal(raw[4:], words)

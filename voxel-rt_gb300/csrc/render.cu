@@ -1118,8 +1118,16 @@ static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, st
             return set_error(VRT_EINVAL, "view %d: bad image", i);
         int st = check_uniforms(&v.uniforms);
         if (st) return st;
-        fill_view(hv[i], v.uniforms, v.width, v.height, v.d_rgba, nullptr, v.d_stats, t, tiles);
-        tiles += tiles_of(v.width, v.height, t);
+        Tuning tv = t;  // a view may choose its own tile shape of the launch's tile size
+        if (v.tile_w > 0 || v.tile_h > 0) {
+            if (v.tile_w < 1 || v.tile_h < 1 || v.tile_w * v.tile_h != t.tile_w * t.tile_h)
+                return set_error(VRT_EINVAL, "view %d: tile %dx%d does not have the launch's %d threads", i, v.tile_w,
+                                 v.tile_h, t.tile_w * t.tile_h);
+            tv.tile_w = v.tile_w;
+            tv.tile_h = v.tile_h;
+        }
+        fill_view(hv[i], v.uniforms, v.width, v.height, v.d_rgba, nullptr, v.d_stats, tv, tiles);
+        tiles += tiles_of(v.width, v.height, tv);
     }
     *world_out = w;
     *total_out = tiles;

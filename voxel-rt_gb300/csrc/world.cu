@@ -10,6 +10,7 @@
 #include <algorithm>
 #include <climits>
 #include <cmath>
+#include <cstdio>
 #include <cstring>
 #include <mutex>
 #include <vector>
@@ -329,6 +330,15 @@ __global__ void fix_depth_field_kernel(int32_t* words, Layout L, int x0, int y0,
     if (nearest < 0.0f) words[idx] = __float_as_int(nearest);
 }
 
+__global__ void probe_kernel(const int32_t* __restrict__ words, Layout L, const int32_t* __restrict__ xyz, int n,
+                             int32_t* __restrict__ out) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int x = xyz[3 * i], y = xyz[3 * i + 1], z = xyz[3 * i + 2];
+    const bool in = x >= 0 && y >= 0 && z >= 0 && x < L.W && y < L.H && z < L.W;
+    out[i] = in ? words[(uint64_t)x + (uint64_t)L.W * y + (uint64_t)L.W * L.H * z] : -1;
+}
+
 // ------------------------------------------------------------------ initVoxels
 
 // level.cpp:85-128: stone/dirt/grass layers, then the holes that placeBush/placeTrunk
@@ -534,6 +544,62 @@ int vrt_world_sync_flags(vrt_world* w, void* stream) {
     VRT_CUDA(cudaStreamSynchronize(S(stream)));
     w->has_depth_field = flag;
     return read_aabb(w, S(stream));
+}
+
+int vrt_world_probe(const vrt_world* w, const int32_t* d_xyz, int32_t n, int32_t* d_words, void* stream) {
+    if (!w || n < 0 || (n > 0 && (!d_xyz || !d_words))) return set_error(VRT_EINVAL, "bad probe arguments");
+    if (n == 0) return VRT_OK;
+    probe_kernel<<<blocks_for((uint64_t)n, 256), 256, 0, S(stream)>>>(w->d_words, w->L, d_xyz, n, d_words);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+static const int32_t kWorldMagic = 0x57525456;  // "VRTW" little-endian
+
+int vrt_world_save(const vrt_world* w, const char* path, void* stream) {
+    if (!w || !path) return set_error(VRT_EINVAL, "NULL argument");
+    std::vector<int32_t> host(w->L.n_words);
+    int st = vrt_world_download(w, host.data(), 0, w->L.n_words, stream);
+    if (st) return st;
+    FILE* f = std::fopen(path, "wb");
+    if (!f) return set_error(VRT_EINVAL, "cannot open %s for writing", path);
+    const int32_t head[4] = {kWorldMagic, 1, w->L.W, w->L.H};
+    bool ok = std::fwrite(head, sizeof(head), 1, f) == 1 &&
+              std::fwrite(host.data(), sizeof(int32_t), host.size(), f) == host.size();
+    ok = (std::fclose(f) == 0) && ok;
+    return ok ? VRT_OK : set_error(VRT_EINVAL, "short write to %s", path);
+}
+
+int vrt_world_load(const char* path, vrt_world** out, void* stream) {
+    if (!path || !out) return set_error(VRT_EINVAL, "NULL argument");
+    *out = nullptr;
+    FILE* f = std::fopen(path, "rb");
+    if (!f) return set_error(VRT_EINVAL, "cannot open %s", path);
+    int32_t head[4] = {0, 0, 0, 0};
+    if (std::fread(head, sizeof(head), 1, f) != 1 || head[0] != kWorldMagic || head[1] != 1) {
+        std::fclose(f);
+        return set_error(VRT_EINVAL, "%s is not a version-1 world file", path);
+    }
+    vrt_world* w = nullptr;
+    int st = vrt_world_create(head[2], head[3], &w);
+    if (st) {
+        std::fclose(f);
+        return st;
+    }
+    std::vector<int32_t> host(w->L.n_words);
+    const bool ok = std::fread(host.data(), sizeof(int32_t), host.size(), f) == host.size();
+    std::fclose(f);
+    if (!ok) {
+        vrt_world_destroy(w);
+        return set_error(VRT_EINVAL, "%s is truncated", path);
+    }
+    st = vrt_world_upload(w, host.data(), 0, host.size(), stream);
+    if (st) {
+        vrt_world_destroy(w);
+        return st;
+    }
+    *out = w;
+    return VRT_OK;
 }
 
 int vrt_place_voxel(vrt_world* w, int32_t x, int32_t y, int32_t z, int32_t word, void* stream) {

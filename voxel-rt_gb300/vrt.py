@@ -102,6 +102,8 @@ class View(C.Structure):
         ("height", C.c_int32),
         ("d_rgba", C.c_void_p),
         ("d_stats", C.c_void_p),
+        ("tile_w", C.c_int32),
+        ("tile_h", C.c_int32),
     ]
 
 
@@ -163,6 +165,9 @@ SIGNATURES = {
     "vrt_world_download": (_I, [_P, _P, _U64, _U64, _P]),
     "vrt_world_download_masks": (_I, [_P, _P, _P, _P, _P]),
     "vrt_world_sync_flags": (_I, [_P, _P]),
+    "vrt_world_probe": (_I, [_P, _P, _I, _P, _P]),
+    "vrt_world_save": (_I, [_P, C.c_char_p, _P]),
+    "vrt_world_load": (_I, [C.c_char_p, C.POINTER(_P), _P]),
     "vrt_remove_sphere": (_I, [_P, _I, _I, _I, _I, _I, _P]),
     "vrt_place_voxel": (_I, [_P, _I, _I, _I, _I, _P]),
     "vrt_fix_depth_field_box": (_I, [_P, _I, _I, _I, _I, _I, _I, _P]),
@@ -300,6 +305,25 @@ class World:
         check(lib().vrt_world_download_masks(self.handle, b.ctypes.data, r.ctypes.data, s.ctypes.data, stream))
         return b, r, s
 
+    def probe(self, d_xyz: int, n: int, d_words: int, stream: int = 0):
+        """Voxel words at n device (x,y,z) int32 triples; -1 outside the world."""
+        check(lib().vrt_world_probe(self.handle, d_xyz, n, d_words, stream))
+
+    def save(self, path: str, stream: int = 0):
+        check(lib().vrt_world_save(self.handle, path.encode(), stream))
+
+    @classmethod
+    def load(cls, path: str, stream: int = 0) -> "World":
+        h = C.c_void_p()
+        check(lib().vrt_world_load(path.encode(), C.byref(h), stream))
+        w = cls.__new__(cls)
+        w.handle = h
+        info = WorldInfo()
+        check(lib().vrt_world_get_info(h, C.byref(info)))
+        w.width, w.height = info.width, info.height
+        w.num_words = w.width * w.height * w.width
+        return w
+
     def sync_flags(self, stream: int = 0) -> int:
         check(lib().vrt_world_sync_flags(self.handle, stream))
         return self.info().has_depth_field
@@ -356,13 +380,16 @@ class Renderer:
                                      C.byref(opts) if opts is not None else None, stream))
 
 
-def make_view(world: World, u: Uniforms, width: int, height: int, d_rgba: int, d_stats: int = 0) -> View:
+def make_view(world: World, u: Uniforms, width: int, height: int, d_rgba: int, d_stats: int = 0,
+              tile=None) -> View:
     v = View()
     v.world = world.handle
     v.uniforms = u
     v.width, v.height = width, height
     v.d_rgba = d_rgba
     v.d_stats = d_stats
+    if tile:
+        v.tile_w, v.tile_h = tile
     return v
 
 
