@@ -126,7 +126,7 @@ typedef struct vrt_world_info {
     int32_t width, height;          /* VOXELS_WIDTH (x and z), VOXELS_HEIGHT (y)      */
     uint64_t num_words;             /* W*H*W                                          */
     const int32_t* d_words;         /* device voxel words                             */
-    const uint64_t* d_brick_mask;   /* device occupancy mask: one uint64 per 4x4x4 brick */
+    const uint64_t* d_brick_mask;   /* device occupancy mask: one uint64 per 4x4x4 brick (linear) */
     const uint64_t* d_region_mask;  /* device: one uint64 per 16x16x16 region, bit per brick */
     int32_t has_depth_field;        /* 1 if any word is < -1 (as of the last sync)    */
     uint64_t device_bytes;          /* device memory held by the world                */
@@ -163,9 +163,12 @@ int vrt_world_upload(vrt_world* w, const int32_t* host_words, uint64_t first, ui
 int vrt_world_upload_device(vrt_world* w, const int32_t* d_words, uint64_t first, uint64_t count, void* stream);
 /* Copy words [first, first+count) back to host memory. */
 int vrt_world_download(const vrt_world* w, int32_t* host_words, uint64_t first, uint64_t count, void* stream);
-/* Copy the occupancy hierarchy to host memory (any pointer may be NULL): bricks hold
- * 64*64*SW*SH*SW words, regions 64*SW*SH*SW, supers SW*SH*SW, with SW = ceil(W/64),
- * SH = ceil(H/64); layout as in vrt_world_info.  Synchronises the stream. */
+/* Copy the occupancy hierarchy to host memory (any pointer may be NULL), SW = ceil(W/64),
+ * SH = ceil(H/64):
+ *   bricks:  64*64*SW*SH*SW words at bx + 16SW*(by + 16SH*bz), voxel bit x+4y+16z (4^3 bricks)
+ *   regions: 64*SW*SH*SW words at super*64 + (rx&3)+4(ry&3)+16(rz&3), bit per brick (16^3)
+ *   supers:  SW*SH*SW words at sx + SW*(sy + SH*sz), bit per region (64^3)
+ * Synchronises the stream. */
 int vrt_world_download_masks(const vrt_world* w, uint64_t* bricks, uint64_t* regions, uint64_t* supers,
                              void* stream);
 /* Batched voxel lookups, the query behind the reference's collision and gravity probes

@@ -118,8 +118,9 @@ def _pack(cells):
 
 def expected_masks(words, W, H):
     """The occupancy hierarchy of a world, in the device's storage order:
-    supers[sx + SW*(sy + SH*sz)], regions[super*64 + local], bricks[region*64 + local],
-    local = x + 4y + 16z of the child inside its parent, voxel bit x + 4y + 16z."""
+    supers[sx + SW*(sy + SH*sz)], regions[super*64 + local], bricks[bx + BWp*(by + BHp*bz)]
+    with BWp = 16*SW, BHp = 16*SH; local = x + 4y + 16z of the child inside its parent,
+    voxel bit x + 4y + 16z."""
     SW, SH = (W + 63) // 64, (H + 63) // 64
     PW, PH = 64 * SW, 64 * SH
     solid = np.zeros((PW, PH, PW), bool)  # [z][y][x]
@@ -129,7 +130,7 @@ def expected_masks(words, W, H):
     S = _pack((R != 0).reshape(SW, 4, SH, 4, SW, 4).transpose(0, 2, 4, 1, 3, 5))
     supers = S.reshape(-1)
     regions = R.reshape(SW, 4, SH, 4, SW, 4).transpose(0, 2, 4, 1, 3, 5).reshape(-1)
-    bricks = B.reshape(SW, 4, 4, SH, 4, 4, SW, 4, 4).transpose(0, 3, 6, 1, 4, 7, 2, 5, 8).reshape(-1)
+    bricks = B.reshape(-1)  # linear: bx + BWp*(by + BHp*bz)
     return bricks, regions, supers
 
 
@@ -137,6 +138,7 @@ def expected_masks_loops(words, W, H):
     """Slow loop form of expected_masks, for checking it on tiny worlds."""
     SW, SH = (W + 63) // 64, (H + 63) // 64
     bricks = np.zeros(64 * 64 * SW * SH * SW, np.uint64)
+    regions = np.zeros(64 * SW * SH * SW, np.uint64)
     for z in range(W):
         for y in range(H):
             for x in range(W):
@@ -147,13 +149,9 @@ def expected_masks_loops(words, W, H):
                 sx, sy, sz = rx >> 2, ry >> 2, rz >> 2
                 si = sx + SW * (sy + SH * sz)
                 ri = si * 64 + (rx & 3) + 4 * (ry & 3) + 16 * (rz & 3)
-                bi = ri * 64 + (bx & 3) + 4 * (by & 3) + 16 * (bz & 3)
+                bi = bx + 16 * SW * (by + 16 * SH * bz)
                 bricks[bi] |= np.uint64(1) << np.uint64((x & 3) + 4 * (y & 3) + 16 * (z & 3))
-    regions = np.zeros(64 * SW * SH * SW, np.uint64)
-    for i in range(regions.size):
-        for c in range(64):
-            if bricks[i * 64 + c]:
-                regions[i] |= np.uint64(1) << np.uint64(c)
+                regions[ri] |= np.uint64(1) << np.uint64((bx & 3) + 4 * (by & 3) + 16 * (bz & 3))
     supers = np.zeros(SW * SH * SW, np.uint64)
     for i in range(supers.size):
         for c in range(64):

@@ -620,8 +620,13 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
         return T_MISS;  // getVoxelIndex == -1 (fshader.glsl:123-125)
     if (!exact && beyond_solids(P, cx, cy, cz, r.sx, r.sy, r.sz)) return T_MISS;
     const int rx = cx >> 4, ry = cy >> 4, rz = cz >> 4;
+    const int bx = cx >> 2, by = cy >> 2, bz = cz >> 2;
     const uint64_t rl = region_linear(L, rx, ry, rz);
+    const uint64_t bidx = brick_index(L, bx, by, bz);
+    // the three loads are independent: issue them together, wait once
     const int dr = SMEM ? (int)rdist[rl] : (int)__ldg(rdist + rl);
+    const uint64_t mb = __ldg(P.bricks + bidx);
+    const int db = __ldg(P.bdist + bidx);
     int lox, loy, loz, hix, hiy, hiz;
     uint64_t m = 0;
     if (dr > 0) {  // every region within Chebyshev radius dr-1 is empty
@@ -629,10 +634,7 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
         lox = (rx - k) << 4; loy = (ry - k) << 4; loz = (rz - k) << 4;
         hix = (rx + k + 1) << 4; hiy = (ry + k + 1) << 4; hiz = (rz + k + 1) << 4;
     } else {
-        const int bx = cx >> 2, by = cy >> 2, bz = cz >> 2;
-        const uint64_t bidx = brick_index(L, bx, by, bz);
-        m = __ldg(P.bricks + bidx);
-        const int db = __ldg(P.bdist + bidx);
+        m = mb;
         const int k = m ? 0 : max(db, 1) - 1;
         lox = (bx - k) << 2; loy = (by - k) << 2; loz = (bz - k) << 2;
         hix = (bx + k + 1) << 2; hiy = (by + k + 1) << 2; hiz = (bz + k + 1) << 2;
@@ -732,7 +734,7 @@ __device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
 // One CTA per ray tile (tile_w x tile_h pixels, tile_w*tile_h == blockDim.x) over the tile
 // space of every view of the launch: a single frame, or a batch of cameras of any sizes.
 template <bool SMEM>
-__global__ void __launch_bounds__(128) render_tiles_kernel(const __grid_constant__ MaskParams P) {
+__global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_constant__ MaskParams P) {
     extern __shared__ __align__(16) uint8_t smem[];
     const uint8_t* rdist = P.rdist;
     if (SMEM) {

@@ -26,9 +26,9 @@ int cuda_error(cudaError_t e, const char* what);
 //   brick  (4x4x4 voxels):   bit (x&3) + 4*(y&3) + 16*(z&3) set when that voxel is solid
 //   region (16x16x16):       bit per brick (bx&3) + 4*(by&3) + 16*(bz&3) set when the brick has a solid voxel
 //   super  (64x64x64):       bit per region, same layout, set when the region has a solid voxel
-// Bricks are stored region-major (64 bricks of a region = 512 contiguous bytes) and
-// regions super-major (64 regions of a super block = 512 bytes), so the nodes a ray
-// visits are close together.  Voxels outside the world count as empty.
+// Bricks are stored linearly, bx + BWp*(by + BHp*bz), so a ray's box lookup computes its
+// brick's slot with two multiply-adds; regions are stored super-major (64 regions of a
+// super block = 512 contiguous bytes).  Voxels outside the world count as empty.
 struct Layout {
     int W, H;           // voxel dims: x,z in [0,W), y in [0,H)
     int RW, RH;         // regions per axis (x/z, y): ceil(W/16), ceil(H/16)
@@ -43,7 +43,7 @@ struct Layout {
 
 // Empty-space distance fields (capped Chebyshev distance, in nodes, to the nearest
 // non-empty node; 0 = the node itself holds a solid voxel):
-//   brick distance: uint8 per brick, stored like the brick masks (node-major);
+//   brick distance: uint8 per brick, stored like the brick masks (linear);
 //   region distance: uint8 per region, linear index rx + RWp*(ry + RHp*rz).
 // A node at distance d >= 1 has every node within Chebyshev radius d-1 empty, so the
 // cube of those nodes is a box a ray can cross without reading voxels.  Values are
@@ -61,9 +61,9 @@ __host__ __device__ inline uint64_t super_index(const Layout& L, int sx, int sy,
 __host__ __device__ inline uint64_t region_index(const Layout& L, int rx, int ry, int rz) {
     return super_index(L, rx >> 2, ry >> 2, rz >> 2) * 64 + ((rx & 3) + 4 * (ry & 3) + 16 * (rz & 3));
 }
-// brick (bx,by,bz) -> slot in the brick array
+// brick (bx,by,bz) -> slot in the brick array (and the brick distance field)
 __host__ __device__ inline uint64_t brick_index(const Layout& L, int bx, int by, int bz) {
-    return region_index(L, bx >> 2, by >> 2, bz >> 2) * 64 + ((bx & 3) + 4 * (by & 3) + 16 * (bz & 3));
+    return (uint64_t)bx + (uint64_t)L.BWp * ((uint64_t)by + (uint64_t)L.BHp * bz);
 }
 
 Layout make_layout(int W, int H);

@@ -110,12 +110,20 @@ __global__ void parent_mask_kernel(const uint64_t* __restrict__ child, uint64_t*
     int py = py0 + (int)((t / npx) % npy);
     int pz = pz0 + (int)(t / ((uint64_t)npx * npy));
     uint64_t slot = level == 1 ? region_index(L, px, py, pz) : super_index(L, px, py, pz);
-    const uint64_t* c = child + slot * 64;
     uint64_t m = 0;
-    for (int i = 0; i < 64; i += 2) {
-        ulonglong2 q = *reinterpret_cast<const ulonglong2*>(c + i);
-        m |= (uint64_t)(q.x != 0) << i;
-        m |= (uint64_t)(q.y != 0) << (i + 1);
+    if (level == 1) {  // the region's 4x4x4 bricks: 16 rows of 4 consecutive slots
+        for (int lz = 0; lz < 4; lz++)
+            for (int ly = 0; ly < 4; ly++) {
+                const uint64_t* row = child + brick_index(L, 4 * px, 4 * py + ly, 4 * pz + lz);
+                for (int lx = 0; lx < 4; lx++) m |= (uint64_t)(row[lx] != 0) << (lx + 4 * ly + 16 * lz);
+            }
+    } else {  // a super block's 64 regions are consecutive
+        const uint64_t* c = child + slot * 64;
+        for (int i = 0; i < 64; i += 2) {
+            ulonglong2 q = *reinterpret_cast<const ulonglong2*>(c + i);
+            m |= (uint64_t)(q.x != 0) << i;
+            m |= (uint64_t)(q.y != 0) << (i + 1);
+        }
     }
     parent[slot] = m;
 }
