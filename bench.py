@@ -286,7 +286,7 @@ def main():
     peak, peak_src = measured_peaks()
     algo_bytes = 4 * steps + 4 * hits + 4 * pixels
     achieved = algo_bytes / (ms * 1e-3) / 1e9
-    kname = {"pixel": "render_mask_pixel_kernel", "mask": "render_mask_kernel", "word": "render_word_kernel"}[args.kernel]
+    kname = {"pixel": "render_tiles_kernel", "mask": "render_mask_kernel", "word": "render_word_kernel"}[args.kernel]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
                 "traffic": load_traffic(kname, "full"), "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": algo_bytes, "kernel": kname,
@@ -375,11 +375,25 @@ def bench_batched(vrt, torch, scenes, sc, world, r, dev, stream):
     b.record(stream)
     torch.cuda.synchronize()
     plain_ms = a.elapsed_time(b) / reps
+    # plain and synchronous: each camera rendered and copied to host before the next
+    host = torch.empty(max(w * h for _, w, h in views) * 4, dtype=torch.uint8, pin_memory=True)
+    for (u, w, h) in views[:4]:
+        r.render_to_host(world, u, w, h, host.data_ptr(), None, sh)
+    t0 = time.perf_counter()
+    for (u, w, h) in views:
+        r.render_to_host(world, u, w, h, host.data_ptr(), None, sh)
+    sync_ms = (time.perf_counter() - t0) * 1e3
     top = sorted(plan.table, key=lambda e: e["ms"])[:4]
     return {"cameras": len(views), "pixels": sum(w * h for _, w, h in views), "rays": rays,
             "batched_ms": batched_ms, "batched_mrays_per_s": rays / (batched_ms * 1e-3) / 1e6,
             "plain_ms": plain_ms, "plain_mrays_per_s": rays / (plain_ms * 1e-3) / 1e6,
-            "speedup": plain_ms / batched_ms, "autotuned": plan.describe(), "autotune_best": top}
+            "speedup": plain_ms / batched_ms,
+            "plain_sync_ms": sync_ms, "plain_sync_mrays_per_s": rays / (sync_ms * 1e-3) / 1e6,
+            "speedup_vs_sync": sync_ms / batched_ms,
+            "note": "plain = one vrt_render launch per camera, back to back on one stream; plain_sync = "
+                    "vrt_render_to_host per camera (render, copy the image to host, wait) -- the batched "
+                    "result is compared without its copies",
+            "autotuned": plan.describe(), "autotune_best": top}
 
 
 def bench_stress(vrt, torch, scenes, dev, stream):
@@ -445,9 +459,40 @@ def bench_served(vrt, torch, scenes, sc, full_world):
         res["rate_hz"] = rate
         results.append(res)
     srv.close()
+    # plain one-request-at-a-time serving of a request stream like the 4000 req/s one: each
+    # render launched, copied to host and waited for; each edit applied and waited for
+    reqs = serving.make_requests(specs, 4000.0, 0.25, seed=7)
+    r = vrt.Renderer()
+    host = torch.empty(1920 * 1080 * 4, dtype=torch.uint8, pin_memory=True)
+    stream = torch.cuda.current_stream().cuda_stream
+    counts = torch.zeros(vrt.STAT_COUNT, dtype=torch.int64, device="cuda")
+    t0 = time.perf_counter()
+    n_render = 0
+    for (_, kind, wi, payload) in reqs:
+        if kind == vrt.REQ_RENDER:
+            u, w, h = payload
+            r.render_to_host(specs[wi].world, u, w, h, host.data_ptr(), None, stream)
+            n_render += 1
+        else:
+            specs[wi].world.remove_sphere(*payload, specs[wi].world.info().has_depth_field, stream)
+            torch.cuda.synchronize()
+    plain_s = time.perf_counter() - t0
+    # the same renders once more with counters, to count their rays
+    for (_, kind, wi, payload) in reqs:
+        if kind == vrt.REQ_RENDER:
+            u, w, h = payload
+            img = torch.empty(w * h * 4, dtype=torch.uint8, device="cuda")
+            r.render(specs[wi].world, u, w, h, img.data_ptr(), None, counts.data_ptr(), None, stream)
+    torch.cuda.synchronize()
+    plain_rays = int(counts[vrt.STAT_RAYS].item())
+    r.close()
     full_world.upload(sc.words)  # the served edits changed the shared world: restore it
+    sat = max(x["mrays_per_s"] for x in results if "mrays_per_s" in x)
     return {"worlds": ["256x256x256", "512x256x512", "1024x256x1024", "1024x256x1024"], "budget_gib": 40,
-            "slots": 4, "max_batch": 8, "sweep": results}
+            "slots": 4, "max_batch": 8, "sweep": results,
+            "plain_sync": {"renders": n_render, "seconds": plain_s, "mrays_per_s": plain_rays / plain_s / 1e6,
+                           "ms_per_render": plain_s * 1e3 / max(n_render, 1)},
+            "served_vs_plain_sync": sat / (plain_rays / plain_s / 1e6)}
 
 
 if __name__ == "__main__":
