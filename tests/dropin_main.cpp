@@ -1,6 +1,6 @@
 // A headless main.cpp on the drop-in render host: the reference's frame loop
 // (main.cpp:58-73) with glDrawArrays replaced by drawFrame().  It renders the reference
-// scene, then destroys a sphere in front of the camera (doDestroy, controls.cpp:100-110)
+// scene, then destroys a sphere on the terrain in view (doDestroy, controls.cpp:100-110)
 // and renders again, writing both frames and the edited world to the output directory.
 #include <cstdio>
 #include <cstring>
@@ -29,14 +29,15 @@ int main(int argc, char** argv) {
     updateUniforms();
     const uint8_t* f0 = drawFrame();
     if (!dump(out + "/frame0.rgba", f0, (size_t)screenWidth * screenHeight * 4)) return 2;
-    // doDestroy: center = camPos + 15 * camDir (camDir = +z), removeSphere(center, 7)
-    const ivec3 c{(int)camPos.x, (int)camPos.y, (int)(camPos.z + 15.0f)};
+    // doDestroy (removeSphere(center, 7)) aimed at the grass surface 30 voxels ahead
+    const ivec3 c{(int)camPos.x, 36, (int)(camPos.z + 30.0f)};
     removeSphere(c, 7);
     updateUniforms();
     const uint8_t* f1 = drawFrame();
     if (!dump(out + "/frame1.rgba", f1, (size_t)screenWidth * screenHeight * 4)) return 2;
     if (!dump(out + "/world1.i32", voxels, (size_t)VOXELS_WIDTH * VOXELS_HEIGHT * VOXELS_WIDTH * 4)) return 2;
-    float params[8] = {camPos.x, camPos.y, camPos.z, lightPos.x, lightPos.y, lightPos.z, aspectRatio, (float)RENDER_DIST};
+    float params[11] = {camPos.x, camPos.y, camPos.z, lightPos.x, lightPos.y, lightPos.z, aspectRatio,
+                        (float)RENDER_DIST, (float)c.x, (float)c.y, (float)c.z};
     if (!dump(out + "/params.f32", params, sizeof(params))) return 2;
     if (vrtStatus() != 0) {
         std::fprintf(stderr, "vrt: %s\n", vrtLastError());

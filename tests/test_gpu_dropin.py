@@ -37,7 +37,7 @@ def test_dropin_main_renders_the_reference_scene(cuda, oracle, tmp_path):
     f0 = np.fromfile(tmp_path / "frame0.rgba", np.uint8).reshape(height, width, 4)
     o0 = oracle.render(world, W, H, u, width, height)
     assert np.array_equal(f0, o0["rgba"])
-    c = [int(params[0]), int(params[1]), int(params[2] + np.float32(15.0))]
+    c = [int(v) for v in params[8:11]]
     oracle.remove_sphere(world, W, H, c[0], c[1], c[2], 7, 1)
     w1 = np.fromfile(tmp_path / "world1.i32", np.int32)
     assert np.array_equal(w1, world)
