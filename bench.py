@@ -192,6 +192,7 @@ def main():
     import torch
 
     import build as vbuild
+    import replicas
     import scenes
     import vrt
 
@@ -259,12 +260,8 @@ def main():
         dist.barrier()
     clk = clocks.stop()
     times = [a.elapsed_time(b) for a, b in evs]
-    ms = sum(times) / len(times)
-    if dist:
-        t = torch.tensor([ms], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        ms = float(t.item())
-    value = world_size * rays / (ms * 1e-3) / 1e6
+    ms = replicas.max_over_ranks(sum(times) / len(times), dist, dev)  # replicas: each rank renders a frame
+    value = replicas.whole_job_rate(rays, ms * 1e-3, world_size) / 1e6
 
     # end to end through the public API: uniforms in, image out to pinned host memory
     host = torch.empty(W * H * 4, dtype=torch.uint8, pin_memory=True)
@@ -275,12 +272,8 @@ def main():
     t0 = time.perf_counter()
     for _ in range(args.steps):
         r.render_to_host(world, sc.uniforms, W, H, host.data_ptr(), opts, sh)
-    e2e_s = (time.perf_counter() - t0) / args.steps
-    if dist:
-        t = torch.tensor([e2e_s], device=dev)
-        dist.all_reduce(t, op=dist.ReduceOp.MAX)
-        e2e_s = float(t.item())
-    e2e = {"value": world_size * rays / e2e_s / 1e6, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
+    e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / args.steps, dist, dev)
+    e2e = {"value": replicas.whole_job_rate(rays, e2e_s, world_size) / 1e6, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
            "h2d_bytes_per_step": int(C_sizeof_uniforms()), "d2h_bytes_per_step": W * H * 4}
 
     peak, peak_src = measured_peaks()
