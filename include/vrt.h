@@ -171,6 +171,16 @@ int vrt_world_download(const vrt_world* w, int32_t* host_words, uint64_t first, 
  * Synchronises the stream. */
 int vrt_world_download_masks(const vrt_world* w, uint64_t* bricks, uint64_t* regions, uint64_t* supers,
                              void* stream);
+/* Copy the empty-space distance fields to host memory (either pointer may be NULL), a
+ * diagnostic with no counterpart in the reference; capped Chebyshev distances, 15 = "15 or more":
+ *   brick_dir:   8 bytes per brick (64*64*SW*SH*SW bricks, ordered like the brick masks);
+ *                byte o is the distance to the nearest non-empty brick in octant o, where
+ *                bit a of o (x=0, y=1, z=2) set means coordinates >= the brick's along a,
+ *                clear means <=
+ *   region_dist: 1 byte per region at rx + 4SW*(ry + 4SH*rz), distance to the nearest
+ *                non-empty region
+ * Synchronises the stream. */
+int vrt_world_download_distances(const vrt_world* w, uint8_t* brick_dir, uint8_t* region_dist, void* stream);
 /* Batched voxel lookups, the query behind the reference's collision and gravity probes
  * (controls.cpp:10-19, :77-98, which read voxels[getVoxelIndex(x,y,z)]): for each of the n
  * device (x,y,z) int32 triples in d_xyz, d_words[i] = the voxel word, or -1 (air) for a

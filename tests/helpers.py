@@ -134,6 +134,87 @@ def expected_masks(words, W, H):
     return bricks, regions, supers
 
 
+def _first_nonempty_cube(occ, signs, centred, cap=15):
+    """For every node of the boolean grid occ [z][y][x]: the smallest k in [0, cap) such
+    that the cube of radius k around the node (centred) or from the node k nodes along
+    `signs` (+1/-1 per axis x, y, z) holds a non-empty node, else cap.  Counts come from a
+    summed-area table, clipped to the grid."""
+    nz, ny, nx = occ.shape
+    sat = np.zeros((nz + 1, ny + 1, nx + 1), np.int64)
+    sat[1:, 1:, 1:] = occ.astype(np.int64).cumsum(0).cumsum(1).cumsum(2)
+    z, y, x = np.meshgrid(np.arange(nz), np.arange(ny), np.arange(nx), indexing="ij")
+    out = np.full(occ.shape, cap, np.uint8)
+    done = np.zeros(occ.shape, bool)
+    for k in range(cap):
+        lo, hi = [], []
+        for c, n, sg in ((x, nx, signs[0]), (y, ny, signs[1]), (z, nz, signs[2])):
+            a = c - k if (centred or sg < 0) else c
+            b = c + k if (centred or sg > 0) else c
+            lo.append(np.clip(a, 0, n - 1))
+            hi.append(np.clip(b, 0, n - 1) + 1)
+        (x0, y0, z0), (x1, y1, z1) = lo, hi
+        cnt = (sat[z1, y1, x1] - sat[z0, y1, x1] - sat[z1, y0, x1] - sat[z1, y1, x0] + sat[z0, y0, x1] +
+               sat[z0, y1, x0] + sat[z1, y0, x0] - sat[z0, y0, x0])
+        new = (cnt > 0) & ~done
+        out[new] = k
+        done |= new
+    return out
+
+
+def expected_distances(words, W, H):
+    """The device's distance fields: (brick_dir, region_dist).  brick_dir holds 8 bytes per
+    brick in brick-mask order; byte o is the capped (15) Chebyshev distance to the nearest
+    non-empty brick in octant o (bit a of o set: coordinates >= the brick's along axis a).
+    region_dist is the capped centred distance of each region, rx + RWp*(ry + RHp*rz)."""
+    bricks, regions, _ = expected_masks(words, W, H)
+    SW, SH = (W + 63) // 64, (H + 63) // 64
+    occ_b = (bricks != 0).reshape(16 * SW, 16 * SH, 16 * SW)  # [bz][by][bx]
+    bdir = np.empty(occ_b.shape + (8,), np.uint8)
+    for o in range(8):
+        signs = tuple(1 if (o >> a) & 1 else -1 for a in range(3))
+        bdir[..., o] = _first_nonempty_cube(occ_b, signs, False)
+    # regions: super*64 + local -> [rz][ry][rx]
+    r = (regions != 0).reshape(SW, SH, SW, 4, 4, 4).transpose(0, 3, 1, 4, 2, 5).reshape(4 * SW, 4 * SH, 4 * SW)
+    rdist = _first_nonempty_cube(r, (1, 1, 1), True)
+    return bdir.reshape(-1), rdist.reshape(-1)
+
+
+def expected_distances_brute(words, W, H):
+    """Brute-force form of expected_distances (every pair of nodes), for tiny worlds."""
+    bricks, regions, _ = expected_masks(words, W, H)
+    SW, SH = (W + 63) // 64, (H + 63) // 64
+    BW, BH = 16 * SW, 16 * SH
+    ne = [(x, y, z) for z in range(BW) for y in range(BH) for x in range(BW) if bricks[x + BW * (y + BH * z)]]
+    bdir = np.full(BW * BH * BW * 8, 15, np.uint8)
+    for z in range(BW):
+        for y in range(BH):
+            for x in range(BW):
+                for (a, b, c) in ne:
+                    d = (a - x, b - y, c - z)
+                    o = (d[0] >= 0) | ((d[1] >= 0) << 1) | ((d[2] >= 0) << 2)
+                    dist = min(15, max(abs(v) for v in d))
+                    # a zero component lies in both half-spaces of its axis
+                    for oo in range(8):
+                        if all(((oo >> i) & 1) == ((o >> i) & 1) or d[i] == 0 for i in range(3)):
+                            j = 8 * (x + BW * (y + BH * z)) + oo
+                            bdir[j] = min(bdir[j], dist)
+    RW, RH = 4 * SW, 4 * SH
+    nr = []
+    for i, m in enumerate(regions):
+        if m:
+            s, l = divmod(i, 64)
+            sx, sy, sz = s % SW, (s // SW) % SH, s // (SW * SH)
+            nr.append((4 * sx + (l & 3), 4 * sy + ((l >> 2) & 3), 4 * sz + (l >> 4)))
+    rdist = np.full(RW * RH * RW, 15, np.uint8)
+    for z in range(RW):
+        for y in range(RH):
+            for x in range(RW):
+                for (a, b, c) in nr:
+                    j = x + RW * (y + RH * z)
+                    rdist[j] = min(rdist[j], min(15, max(abs(a - x), abs(b - y), abs(c - z))))
+    return bdir, rdist
+
+
 def expected_masks_loops(words, W, H):
     """Slow loop form of expected_masks, for checking it on tiny worlds."""
     SW, SH = (W + 63) // 64, (H + 63) // 64

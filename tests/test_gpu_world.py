@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 import vrt
-from helpers import expected_masks, load_golden, make_world
+from helpers import expected_distances, expected_masks, load_golden, make_world
 
 pytestmark = pytest.mark.gpu
 
@@ -22,6 +22,38 @@ def check_masks(w: vrt.World, words):
     assert np.array_equal(s, es), "super masks"
     assert np.array_equal(r, er), "region masks"
     assert np.array_equal(b, eb), "brick masks"
+
+
+def check_distances(w: vrt.World, words):
+    bd, rd = w.distances()
+    ebd, erd = expected_distances(words, w.width, w.height)
+    assert np.array_equal(rd, erd), "region distances"
+    assert np.array_equal(bd, ebd), "directed brick distances"
+
+
+def test_distance_fields_follow_edits(cuda, vrt_lib):
+    # a world wider than twice the distance cap (48 bricks), so an edit refreshes only the
+    # bricks around it: every field must still equal a from-scratch computation
+    W, H = 192, 64
+    rng = np.random.default_rng(12)
+    words = np.where(rng.random(W * H * W) < 0.0004, 0x01102030, -1).astype(np.int32)
+    w = make_world(words, W, H)
+    check_distances(w, words)
+    w.remove_sphere(40, 30, 40, 9, 0)
+    words = w.download(np.empty_like(words))
+    check_distances(w, words)
+    for (x, y, z) in [(3, 3, 3), (180, 60, 7), (100, 0, 190), (96, 32, 96)]:
+        w.place_voxel(x, y, z, 0x01FFFFFF)
+        words[x + W * y + W * H * z] = 0x01FFFFFF
+        check_distances(w, words)
+    patch = np.full(150, 0x01445566, np.int32)
+    first = 20 + W * 10 + W * H * 150
+    w.upload(patch, first)
+    words[first:first + 150] = patch
+    check_distances(w, words)
+    empty = make_world(np.full(64 * 64 * 64, -1, np.int32), 64, 64)
+    bd, rd = empty.distances()
+    assert (bd == 15).all() and (rd == 15).all()
 
 
 def test_init_reference_matches_reference(cuda):
@@ -67,6 +99,7 @@ def test_edits_on_generated_world_match_oracle(cuda, oracle, vrt_lib):
     assert np.array_equal(got, ref)
     assert w.info().has_depth_field == 0
     check_masks(w, got)
+    check_distances(w, got)
 
 
 def test_partial_upload_refreshes_masks(cuda, vrt_lib):
@@ -80,6 +113,7 @@ def test_partial_upload_refreshes_masks(cuda, vrt_lib):
     got = w.download(np.empty_like(words))
     assert np.array_equal(got, words)
     check_masks(w, words)
+    check_distances(w, words)
     # a depth-field word raises the flag, so AUTO renders with the word kernel
     w.upload(np.array([np.float32(-3.0).view(np.int32)], np.int32), 7)
     assert w.info().has_depth_field == 1

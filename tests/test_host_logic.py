@@ -4,7 +4,7 @@ import math
 
 import numpy as np
 
-from helpers import expected_masks, expected_masks_loops
+from helpers import expected_distances, expected_distances_brute, expected_masks, expected_masks_loops
 
 
 def test_mask_layout_model_matches_loops():
@@ -13,6 +13,19 @@ def test_mask_layout_model_matches_loops():
         words = np.where(rng.random(W * H * W) < 0.01, 5, -1).astype(np.int32)
         for a, b in zip(expected_masks(words, W, H), expected_masks_loops(words, W, H)):
             assert np.array_equal(a, b)
+
+
+def test_distance_field_model_matches_brute_force():
+    # a few solid voxels in a tiny world: the summed-area model of the directed brick
+    # distances and the region distances equals the pairwise minimum
+    rng = np.random.default_rng(8)
+    W, H = 24, 12
+    words = np.where(rng.random(W * H * W) < 0.0015, 5, -1).astype(np.int32)
+    words[0] = 7
+    bd, rd = expected_distances(words, W, H)
+    bb, rb = expected_distances_brute(words, W, H)
+    assert np.array_equal(bd, bb) and np.array_equal(rd, rb)
+    assert bd.max() == 15 and (bd == 0).sum() == 8 * (expected_masks(words, W, H)[0] != 0).sum()
 
 
 def test_uniform_defaults_are_the_reference_constants(vrt_lib):

@@ -189,9 +189,10 @@ struct ViewDev {
 struct MaskParams {
     const int32_t* words;
     const uint64_t* bricks;
-    const uint8_t* bdist;
+    const uint8_t* bdir;   // directed brick distances, 8 bytes per brick (one per octant)
     const uint8_t* rdist;
     int bb[6];             // solid bounding box: min x,y,z, max x,y,z (never smaller than the truth)
+    int cl[6];             // tile kernel: boxes are clipped to [cl[0],cl[3]) x [cl[1],cl[4]) x [cl[2],cl[5])
     Layout L;
     const ViewDev* views;  // nviews entries (device); NULL when nviews == 1 (v0 is used)
     int nviews;
@@ -275,7 +276,8 @@ __device__ __forceinline__ int refill(Ray& r, const MaskParams& P, const uint8_t
         const int bx = r.cx >> 2, by = r.cy >> 2, bz = r.cz >> 2;
         const uint64_t bi = brick_index(L, bx, by, bz);
         m = __ldg(P.bricks + bi);
-        const int db = __ldg(P.bdist + bi);
+        const int oct = (r.sx > 0) | ((r.sy > 0) << 1) | ((r.sz > 0) << 2);
+        const int db = __ldg(P.bdir + bi * 8 + oct);
         const int k = m ? 0 : max(db, 1) - 1;
         lox = (bx - k) << 2; loy = (by - k) << 2; loz = (bz - k) << 2;
         hix = (bx + k + 1) << 2; hiy = (by + k + 1) << 2; hiz = (bz + k + 1) << 2;
@@ -612,24 +614,26 @@ __device__ __forceinline__ void set_axis(int c, int s, int lo, int hi, int& k, i
 // The ray stands in cell c, outside any known box: bound the largest empty box around
 // c from the distance fields, or load c's brick.  Returns T_LIVE, T_HIT (c is solid) or
 // T_MISS (c is outside the world).
-template <bool SMEM>
-__device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, const MaskParams& P,
-                                         const uint8_t* rdist, bool exact) {
+template <bool EXACT>
+__device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, const MaskParams& P) {
     const Layout& L = P.L;
     if ((unsigned)cx >= (unsigned)L.W || (unsigned)cy >= (unsigned)L.H || (unsigned)cz >= (unsigned)L.W)
         return T_MISS;  // getVoxelIndex == -1 (fshader.glsl:123-125)
-    if (!exact && beyond_solids(P, cx, cy, cz, r.sx, r.sy, r.sz)) return T_MISS;
+    if (!EXACT && beyond_solids(P, cx, cy, cz, r.sx, r.sy, r.sz)) return T_MISS;
     const int rx = cx >> 4, ry = cy >> 4, rz = cz >> 4;
     const int bx = cx >> 2, by = cy >> 2, bz = cz >> 2;
     const uint64_t rl = region_linear(L, rx, ry, rz);
     const uint64_t bidx = brick_index(L, bx, by, bz);
     // the three loads are independent: issue them together, wait once
-    const int dr = SMEM ? (int)rdist[rl] : (int)__ldg(rdist + rl);
+    const int dr = __ldg(P.rdist + rl);
     const uint64_t mb = __ldg(P.bricks + bidx);
-    const int db = __ldg(P.bdist + bidx);
+    const int oct = (r.sx > 0) | ((r.sy > 0) << 1) | ((r.sz > 0) << 2);
+    const int db = __ldg(P.bdir + bidx * 8 + oct);
     int lox, loy, loz, hix, hiy, hiz;
     uint64_t m = 0;
-    if (dr > 0) {  // every region within Chebyshev radius dr-1 is empty
+    // every region within Chebyshev radius dr-1 is empty: take that cube unless the
+    // brick's directed cube (db bricks ahead) reaches at least as far
+    if (dr > 0 && (dr << 2) > db) {
         const int k = dr - 1;
         lox = (rx - k) << 4; loy = (ry - k) << 4; loz = (rz - k) << 4;
         hix = (rx + k + 1) << 4; hiy = (ry + k + 1) << 4; hiz = (rz + k + 1) << 4;
@@ -639,8 +643,10 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
         lox = (bx - k) << 2; loy = (by - k) << 2; loz = (bz - k) << 2;
         hix = (bx + k + 1) << 2; hiy = (by + k + 1) << 2; hiz = (bz + k + 1) << 2;
     }
-    lox = max(lox, 0); loy = max(loy, 0); loz = max(loz, 0);
-    hix = min(hix, L.W); hiy = min(hiy, L.H); hiz = min(hiz, L.W);
+    // clip to the world, and for inexact launches to the solid box too: a ray that
+    // leaves the solid box along its direction of travel then ends at the next lookup
+    lox = max(lox, P.cl[0]); loy = max(loy, P.cl[1]); loz = max(loz, P.cl[2]);
+    hix = min(hix, P.cl[3]); hiy = min(hiy, P.cl[4]); hiz = min(hiz, P.cl[5]);
     set_axis(cx, r.sx, lox, hix, r.kx, r.ex);
     set_axis(cy, r.sy, loy, hiy, r.ky, r.ey);
     set_axis(cz, r.sz, loz, hiz, r.kz, r.ez);
@@ -653,10 +659,9 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
 // shader's comparison and its one intersect add, in the shader's order; memory is read
 // only when the ray leaves its known box.  On a hit, cd / axis / sgn / cell describe the
 // last step (currDist, hitNormal, the voxel).
-template <bool SMEM>
-__device__ __forceinline__ int cast_box(const MaskParams& P, const uint8_t* rdist, bool exact, V3 o,
-                                        V3 d, int n, int maxSteps, float& cd, int& axis, int& sgn, int& steps,
-                                        int32_t& hit_index, unsigned& refills) {
+template <bool EXACT>
+__device__ __forceinline__ int cast_box(const MaskParams& P, V3 o, V3 d, int n, int maxSteps, float& cd, int& axis,
+                                        int& sgn, int& steps, int32_t& hit_index, unsigned& refills) {
     RaySetup s;
     ray_setup(o, d, s);
     BoxRay r;
@@ -692,7 +697,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const uint8_t* rdis
             if (out) {
                 refills++;
                 const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
-                const int t = enter_box<SMEM>(r, cx, cy, cz, P, rdist, exact);
+                const int t = enter_box<EXACT>(r, cx, cy, cz, P);
                 if (t == T_HIT) { result = T_HIT; hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz; }
                 else if (t == T_MISS) result = T_MISS;
                 else result = T_LIVE;
@@ -733,17 +738,9 @@ __device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
 
 // One CTA per ray tile (tile_w x tile_h pixels, tile_w*tile_h == blockDim.x) over the tile
 // space of every view of the launch: a single frame, or a batch of cameras of any sizes.
-template <bool SMEM>
+// EXACT launches (any view asking for step counts) step every ray to its end.
+template <bool EXACT>
 __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_constant__ MaskParams P) {
-    extern __shared__ __align__(16) uint8_t smem[];
-    const uint8_t* rdist = P.rdist;
-    if (SMEM) {
-        const uint4* src = reinterpret_cast<const uint4*>(P.rdist);
-        uint4* dst = reinterpret_cast<uint4*>(smem);
-        for (int i = threadIdx.x; i < P.region_bytes16 / 16; i += blockDim.x) dst[i] = __ldg(src + i);
-        __syncthreads();
-        rdist = smem;
-    }
     const int tile = blockIdx.x;
     const ViewDev& V = view_of(P, view_of_tile(P, tile));
     const int lt = tile - V.tile_begin;
@@ -759,8 +756,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
         float cd = 0.f, c2;
         int axis = 2, sgn = 0, steps = 0, a2, s2;
         int32_t hit = -1, dummy = -1;
-        const bool exact = V.exact != 0;
-        const int pr = cast_box<SMEM>(P, rdist, exact, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit,
+        const int pr = cast_box<EXACT>(P, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit,
                                       refills);
         res.primary_steps = steps;
         float mr = u.ambient, mg = u.ambient, mb = u.ambient;
@@ -771,7 +767,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
             const V3 hp = add3(mul3s(rd, cd), cam);
             const V3 hn = axis_normal(axis, sgn);
             const V3 toLight = norm3(sub3(V3{u.lightPos[0], u.lightPos[1], u.lightPos[2]}, hp));
-            const int sr = cast_box<SMEM>(P, rdist, exact, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
+            const int sr = cast_box<EXACT>(P, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
                                           u.maxSteps, c2, a2, s2, steps, dummy, refills);
             res.cast |= 1u;
             if (sr != T_HIT) {
@@ -795,7 +791,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
                     const float ld = len3(dl);
                     if (ld <= R) {
                         const V3 tl = norm3(dl);
-                        const int lr = cast_box<SMEM>(P, rdist, exact, add3(hp, mul3s(tl, 0.001f)), tl,
+                        const int lr = cast_box<EXACT>(P, add3(hp, mul3s(tl, 0.001f)), tl,
                                                       f2i(fadd(ld, 1.0f)), u.maxSteps, c2, a2, s2, steps, dummy,
                                                       refills);
                         res.cast |= 2u << i;
@@ -930,7 +926,7 @@ static int launch_mask(vrt_renderer* r, const vrt_world* w, const ViewDev* h_vie
     std::memset(&P, 0, sizeof(P));
     P.words = w->d_words;
     P.bricks = w->d_bricks;
-    P.bdist = w->d_bdist;
+    P.bdir = w->d_bdir;
     P.rdist = w->d_rdist;
     std::memcpy(P.bb, w->h_aabb, sizeof(P.bb));
     P.L = w->L;
@@ -965,7 +961,7 @@ static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, 
     std::memset(&P, 0, sizeof(P));
     P.words = w->d_words;
     P.bricks = w->d_bricks;
-    P.bdist = w->d_bdist;
+    P.bdir = w->d_bdir;
     P.rdist = w->d_rdist;
     std::memcpy(P.bb, w->h_aabb, sizeof(P.bb));
     P.L = w->L;
@@ -973,10 +969,15 @@ static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, 
     P.nviews = nviews;
     P.total_tiles = total_tiles;
     P.v0 = h_views[0];
-    const int region_bytes = w->L.RWp * w->L.RHp * w->L.RWp;
-    P.region_bytes16 = (region_bytes + 15) & ~15;
+    bool exact = false;
+    for (int i = 0; i < nviews; i++) exact |= h_views[i].exact != 0;
+    const int dims[3] = {w->L.W, w->L.H, w->L.W};
+    for (int a = 0; a < 3; a++) {
+        P.cl[a] = exact ? 0 : std::max(0, std::min(P.bb[a], dims[a]));
+        P.cl[3 + a] = exact ? dims[a] : std::min(dims[a], std::max(P.bb[3 + a] + 1, P.cl[a]));
+    }
     // region distances are read through L1 (staging them per CTA costs more than it saves)
-    auto kern = render_tiles_kernel<false>;
+    auto kern = exact ? render_tiles_kernel<true> : render_tiles_kernel<false>;
     if (total_tiles > 0) kern<<<total_tiles, threads, 0, s>>>(P);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;

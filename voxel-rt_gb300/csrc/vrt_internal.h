@@ -42,13 +42,21 @@ struct Layout {
 };
 
 // Empty-space distance fields (capped Chebyshev distance, in nodes, to the nearest
-// non-empty node; 0 = the node itself holds a solid voxel):
-//   brick distance: uint8 per brick, stored like the brick masks (linear);
-//   region distance: uint8 per region, linear index rx + RWp*(ry + RHp*rz).
-// A node at distance d >= 1 has every node within Chebyshev radius d-1 empty, so the
-// cube of those nodes is a box a ray can cross without reading voxels.  Values are
-// capped (never larger than the truth), and recomputed whenever solids may be added.
+// non-empty node; 0 = the node itself holds a solid voxel).  Values are capped (never
+// larger than the truth) and recomputed whenever solids may be added.
+//   region distance: uint8 per region, linear index rx + RWp*(ry + RHp*rz).  A region at
+//   distance d >= 1 has every region within Chebyshev radius d-1 empty, so the cube of
+//   those regions is a box a ray can cross without reading voxels.
 constexpr int kDistCap = 15;
+
+// Directed brick distances: 8 bytes per brick, stored like the brick masks.  Byte o
+// (octant o: bit a set = the + direction along axis a, x=0 y=1 z=2) is the capped
+// Chebyshev distance from the brick to the nearest non-empty brick n in that octant
+// (n_a >= b_a where bit a is set, n_a <= b_a where it is clear).  At distance d >= 1
+// the cube of bricks from b to b + (d-1) in the octant's directions is empty: a ray
+// moving into that octant leaves its brick only through that cube's far faces, so the
+// cube bounds it as well as a centred cube of the same radius would, while solids
+// behind or beside the ray no longer shrink it.
 
 __host__ __device__ inline uint64_t region_linear(const Layout& L, int rx, int ry, int rz) {
     return (uint64_t)rx + (uint64_t)L.RWp * ((uint64_t)ry + (uint64_t)L.RHp * rz);
@@ -76,9 +84,9 @@ struct vrt_world {
     uint64_t* d_bricks = nullptr;
     uint64_t* d_regions = nullptr;
     uint64_t* d_supers = nullptr;
-    uint8_t* d_bdist = nullptr;     // brick distance field (node-major, n_bricks)
     uint8_t* d_rdist = nullptr;     // region distance field (linear, RWp*RHp*RWp)
-    uint8_t* d_tmp_a = nullptr;     // scratch of the distance passes (n_bricks each)
+    uint8_t* d_bdir = nullptr;      // directed brick distances (8 bytes per brick, linear)
+    uint8_t* d_tmp_a = nullptr;     // scratch of the distance passes (8 * n_bricks each)
     uint8_t* d_tmp_b = nullptr;
     int* d_flag = nullptr;          // has-depth-field flag written by the mask kernels
     int* d_aabb = nullptr;          // bounding box of the solid voxels, brick-granular and

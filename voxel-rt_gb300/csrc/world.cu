@@ -130,70 +130,105 @@ __global__ void parent_mask_kernel(const uint64_t* __restrict__ child, uint64_t*
 
 static inline unsigned blocks_for(uint64_t n, int threads) { return (unsigned)((n + threads - 1) / threads); }
 
-// One 1-D pass of the capped Chebyshev distance transform over the box
-// [x0,x0+nx) x [y0,y0+ny) x [z0,z0+nz) of the brick (level 0) or region (level 1) grid:
+// One 1-D pass of the capped Chebyshev distance transform over the region grid:
 //   out(p) = min over |k| <= cap of max(|k|, in(p + k e_axis)),
-// where in() of the first pass is 0 for a non-empty node and cap+1 for an empty one, and
-// nodes outside the padded grid are empty.  Three passes (x, y, z) give the L-inf distance.
+// where in() of the first pass is 0 for a non-empty region and cap+1 for an empty one, and
+// regions outside the padded grid are empty.  Three passes (x, y, z) give the L-inf distance.
 __global__ void cheb_pass_kernel(const uint64_t* __restrict__ occ, const uint8_t* __restrict__ in,
-                                 uint8_t* __restrict__ out, Layout L, int level, int axis, int x0, int y0, int z0,
-                                 int nx, int ny, int nz, int first) {
+                                 uint8_t* __restrict__ out, Layout L, int axis, int first) {
+    const int DX = L.RWp, DY = L.RHp;
     uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= (uint64_t)nx * ny * nz) return;
-    const int x = x0 + (int)(t % nx), y = y0 + (int)((t / nx) % ny), z = z0 + (int)(t / ((uint64_t)nx * ny));
-    const int DX = level == 0 ? L.BWp : L.RWp, DY = level == 0 ? L.BHp : L.RHp;
+    if (t >= (uint64_t)DX * DY * DX) return;
+    const int x = (int)(t % DX), y = (int)((t / DX) % DY), z = (int)(t / ((uint64_t)DX * DY));
     const int cap = kDistCap;
     int best = cap + 1;
     for (int k = -cap; k <= cap; k++) {
         int qx = x + (axis == 0 ? k : 0), qy = y + (axis == 1 ? k : 0), qz = z + (axis == 2 ? k : 0);
         if (qx < 0 || qy < 0 || qz < 0 || qx >= DX || qy >= DY || qz >= DX) continue;
-        int v;
-        if (first) {
-            uint64_t oi = level == 0 ? brick_index(L, qx, qy, qz) : region_index(L, qx, qy, qz);
-            v = occ[oi] != 0 ? 0 : cap + 1;
-        } else {
-            v = in[level == 0 ? brick_index(L, qx, qy, qz) : region_linear(L, qx, qy, qz)];
-        }
+        const int v = first ? (occ[region_index(L, qx, qy, qz)] != 0 ? 0 : cap + 1) : in[region_linear(L, qx, qy, qz)];
         int a = k < 0 ? -k : k;
         best = min(best, max(a, v));
     }
-    out[level == 0 ? brick_index(L, x, y, z) : region_linear(L, x, y, z)] = (uint8_t)min(best, cap);
+    out[region_linear(L, x, y, z)] = (uint8_t)min(best, cap);
 }
 
-static int dist_passes(vrt_world* w, int level, int bx0, int by0, int bz0, int bx1, int by1, int bz1,
-                       cudaStream_t s) {
+// One axis pass of the directed brick distances, all eight octants at once (one byte
+// each): out_o(b) = min over j in [0, cap] of max(j, in_o(b + sgn_o * j * e_axis)), where
+// sgn_o is + for octants with bit `axis` set.  The first pass reads occupancy (0 for a
+// non-empty brick, cap otherwise).  Bytes are processed four at a time with the SIMD
+// byte min/max intrinsics; values never exceed the cap, which stands for "cap or more".
+__global__ void dir_pass_kernel(const uint64_t* __restrict__ occ, const uint64_t* __restrict__ in,
+                                uint64_t* __restrict__ out, Layout L, int axis, int x0, int y0, int z0, int nx,
+                                int ny, int nz, int first) {
+    uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)nx * ny * nz) return;
+    const int x = x0 + (int)(t % nx), y = y0 + (int)((t / nx) % ny), z = z0 + (int)(t / ((uint64_t)nx * ny));
+    const int c = axis == 0 ? x : (axis == 1 ? y : z);
+    const int D = axis == 1 ? L.BHp : L.BWp;
+    const int64_t stride = axis == 0 ? 1 : (axis == 1 ? (int64_t)L.BWp : (int64_t)L.BWp * L.BHp);
+    const int64_t self = (int64_t)brick_index(L, x, y, z);
+    const uint32_t capb = 0x01010101u * kDistCap;
+    uint64_t res[2];
+    for (int d = 0; d < 2; d++) {
+        const int sg = d == 0 ? 1 : -1;
+        uint32_t lo = capb, hi = capb;
+        for (int j = 0; j <= kDistCap; j++) {
+            const int q = c + sg * j;
+            if (q < 0 || q >= D) break;
+            const int64_t qi = self + sg * j * stride;
+            const uint64_t v = first ? (occ[qi] ? 0ull : ((uint64_t)capb << 32 | capb)) : in[qi];
+            const uint32_t jj = 0x01010101u * (uint32_t)j;
+            lo = __vminu4(lo, __vmaxu4((uint32_t)v, jj));
+            hi = __vminu4(hi, __vmaxu4((uint32_t)(v >> 32), jj));
+            if (__vcmpleu4(lo, jj) == 0xFFFFFFFFu && __vcmpleu4(hi, jj) == 0xFFFFFFFFu) break;  // nothing drops below j
+        }
+        res[d] = (uint64_t)hi << 32 | lo;
+    }
+    const uint64_t plus = axis == 0 ? 0xFF00FF00FF00FF00ull : (axis == 1 ? 0xFFFF0000FFFF0000ull : 0xFFFFFFFF00000000ull);
+    out[self] = (res[0] & plus) | (res[1] & ~plus);
+}
+
+static int dir_passes(vrt_world* w, int bx0, int by0, int bz0, int bx1, int by1, int bz1, cudaStream_t s) {
     const Layout& L = w->L;
     const int cap = kDistCap;
-    const int DX = level == 0 ? L.BWp : L.RWp, DY = level == 0 ? L.BHp : L.RHp;
     auto clampbox = [&](int& a0, int& a1, int lim) { a0 = std::max(a0, 0); a1 = std::min(a1, lim); };
-    // the z pass writes B; the y pass must cover B grown by cap in z; the x pass B grown in y and z
     int X0 = bx0, X1 = bx1, Y0 = by0, Y1 = by1, Z0 = bz0, Z1 = bz1;
-    clampbox(X0, X1, DX); clampbox(Y0, Y1, DY); clampbox(Z0, Z1, DX);
+    clampbox(X0, X1, L.BWp); clampbox(Y0, Y1, L.BHp); clampbox(Z0, Z1, L.BWp);
     if (X0 >= X1 || Y0 >= Y1 || Z0 >= Z1) return VRT_OK;
     int ya0 = Y0 - cap, ya1 = Y1 + cap, za0 = Z0 - cap, za1 = Z1 + cap;
-    clampbox(ya0, ya1, DY); clampbox(za0, za1, DX);
-    const uint64_t* occ = level == 0 ? w->d_bricks : w->d_regions;
-    uint8_t* dst = level == 0 ? w->d_bdist : w->d_rdist;
+    clampbox(ya0, ya1, L.BHp); clampbox(za0, za1, L.BWp);
+    uint64_t* ta = reinterpret_cast<uint64_t*>(w->d_tmp_a);
+    uint64_t* tb = reinterpret_cast<uint64_t*>(w->d_tmp_b);
     uint64_t n = (uint64_t)(X1 - X0) * (ya1 - ya0) * (za1 - za0);
-    cheb_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(occ, nullptr, w->d_tmp_a, L, level, 0, X0, ya0, za0, X1 - X0,
-                                                        ya1 - ya0, za1 - za0, 1);
+    dir_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_bricks, nullptr, ta, L, 0, X0, ya0, za0, X1 - X0,
+                                                       ya1 - ya0, za1 - za0, 1);
     n = (uint64_t)(X1 - X0) * (Y1 - Y0) * (za1 - za0);
-    cheb_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(occ, w->d_tmp_a, w->d_tmp_b, L, level, 1, X0, Y0, za0,
-                                                        X1 - X0, Y1 - Y0, za1 - za0, 0);
+    dir_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_bricks, ta, tb, L, 1, X0, Y0, za0, X1 - X0, Y1 - Y0,
+                                                       za1 - za0, 0);
     n = (uint64_t)(X1 - X0) * (Y1 - Y0) * (Z1 - Z0);
-    cheb_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(occ, w->d_tmp_b, dst, L, level, 2, X0, Y0, Z0, X1 - X0,
-                                                        Y1 - Y0, Z1 - Z0, 0);
+    dir_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_bricks, tb, reinterpret_cast<uint64_t*>(w->d_bdir), L,
+                                                       2, X0, Y0, Z0, X1 - X0, Y1 - Y0, Z1 - Z0, 0);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
 
-// Distances of every brick within kDistCap bricks of the changed brick box, and of all
-// regions (a few thousand to a few hundred thousand bytes).
+static int region_passes(vrt_world* w, cudaStream_t s) {
+    const Layout& L = w->L;
+    const uint64_t n = (uint64_t)L.RWp * L.RHp * L.RWp;
+    cheb_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_regions, nullptr, w->d_tmp_a, L, 0, 1);
+    cheb_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_regions, w->d_tmp_a, w->d_tmp_b, L, 1, 0);
+    cheb_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_regions, w->d_tmp_b, w->d_rdist, L, 2, 0);
+    VRT_CUDA(cudaGetLastError());
+    return VRT_OK;
+}
+
+// Directed distances of every brick within kDistCap bricks of the changed brick box, and
+// the distances of all regions (a few thousand to a few hundred thousand bytes).
 static int refresh_distances(vrt_world* w, int bx0, int by0, int bz0, int bx1, int by1, int bz1, cudaStream_t s) {
     const int cap = kDistCap;
-    int st = dist_passes(w, 0, bx0 - cap, by0 - cap, bz0 - cap, bx1 + cap, by1 + cap, bz1 + cap, s);
+    int st = dir_passes(w, bx0 - cap, by0 - cap, bz0 - cap, bx1 + cap, by1 + cap, bz1 + cap, s);
     if (st) return st;
-    return dist_passes(w, 1, 0, 0, 0, w->L.RWp, w->L.RHp, w->L.RWp, s);
+    return region_passes(w, s);
 }
 
 int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int z1, cudaStream_t s) {
@@ -426,24 +461,24 @@ int vrt_world_create(int32_t width, int32_t height, vrt_world** out) {
     vrt_world* w = new vrt_world();
     w->L = make_layout(width, height);
     cudaGetDevice(&w->device);
-    uint64_t bytes = w->L.n_words * 4 + (w->L.n_bricks + w->L.n_regions + w->L.n_supers) * 8 + 3 * w->L.n_bricks +
+    uint64_t bytes = w->L.n_words * 4 + (w->L.n_bricks + w->L.n_regions + w->L.n_supers) * 8 + 24 * w->L.n_bricks +
                      (uint64_t)w->L.RWp * w->L.RHp * w->L.RWp + 256;
     cudaError_t e = cudaMalloc(&w->d_words, w->L.n_words * 4);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_bricks, w->L.n_bricks * 8);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_regions, w->L.n_regions * 8);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_supers, w->L.n_supers * 8);
-    if (e == cudaSuccess) e = cudaMalloc(&w->d_bdist, w->L.n_bricks);
     const uint64_t rbytes = ((uint64_t)w->L.RWp * w->L.RHp * w->L.RWp + 15) & ~(uint64_t)15;  // staged as uint4
     if (e == cudaSuccess) e = cudaMalloc(&w->d_rdist, rbytes);
-    if (e == cudaSuccess) e = cudaMalloc(&w->d_tmp_a, w->L.n_bricks);
-    if (e == cudaSuccess) e = cudaMalloc(&w->d_tmp_b, w->L.n_bricks);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_bdir, w->L.n_bricks * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_tmp_a, w->L.n_bricks * 8);
+    if (e == cudaSuccess) e = cudaMalloc(&w->d_tmp_b, w->L.n_bricks * 8);
     if (e == cudaSuccess) e = cudaMalloc(&w->d_flag, sizeof(int));
     if (e == cudaSuccess) e = cudaMalloc(&w->d_aabb, 8 * sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(w->d_words, 0xFF, w->L.n_words * 4);  // air = -1 (render.cpp:349-351)
     if (e == cudaSuccess) e = cudaMemset(w->d_bricks, 0, w->L.n_bricks * 8);
     if (e == cudaSuccess) e = cudaMemset(w->d_regions, 0, w->L.n_regions * 8);
     if (e == cudaSuccess) e = cudaMemset(w->d_supers, 0, w->L.n_supers * 8);
-    if (e == cudaSuccess) e = cudaMemset(w->d_bdist, kDistCap, w->L.n_bricks);  // an all-air world
+    if (e == cudaSuccess) e = cudaMemset(w->d_bdir, kDistCap, w->L.n_bricks * 8);  // an all-air world
     if (e == cudaSuccess) e = cudaMemset(w->d_rdist, kDistCap, rbytes);
     if (e == cudaSuccess) e = cudaMemset(w->d_flag, 0, sizeof(int));
     if (e == cudaSuccess) {  // an all-air world: empty box (min > max)
@@ -469,8 +504,8 @@ int vrt_world_destroy(vrt_world* w) {
     cudaFree(w->d_bricks);
     cudaFree(w->d_regions);
     cudaFree(w->d_supers);
-    cudaFree(w->d_bdist);
     cudaFree(w->d_rdist);
+    cudaFree(w->d_bdir);
     cudaFree(w->d_tmp_a);
     cudaFree(w->d_tmp_b);
     cudaFree(w->d_flag);
@@ -536,6 +571,17 @@ int vrt_world_download_masks(const vrt_world* w, uint64_t* bricks, uint64_t* reg
         VRT_CUDA(cudaMemcpyAsync(regions, w->d_regions, w->L.n_regions * 8, cudaMemcpyDeviceToHost, S(stream)));
     if (supers)
         VRT_CUDA(cudaMemcpyAsync(supers, w->d_supers, w->L.n_supers * 8, cudaMemcpyDeviceToHost, S(stream)));
+    VRT_CUDA(cudaStreamSynchronize(S(stream)));
+    return VRT_OK;
+}
+
+int vrt_world_download_distances(const vrt_world* w, uint8_t* brick_dir, uint8_t* region_dist, void* stream) {
+    if (!w) return set_error(VRT_EINVAL, "NULL world");
+    if (brick_dir)
+        VRT_CUDA(cudaMemcpyAsync(brick_dir, w->d_bdir, w->L.n_bricks * 8, cudaMemcpyDeviceToHost, S(stream)));
+    if (region_dist)
+        VRT_CUDA(cudaMemcpyAsync(region_dist, w->d_rdist, (uint64_t)w->L.RWp * w->L.RHp * w->L.RWp,
+                                 cudaMemcpyDeviceToHost, S(stream)));
     VRT_CUDA(cudaStreamSynchronize(S(stream)));
     return VRT_OK;
 }

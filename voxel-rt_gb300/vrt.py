@@ -164,6 +164,7 @@ SIGNATURES = {
     "vrt_world_upload_device": (_I, [_P, _P, _U64, _U64, _P]),
     "vrt_world_download": (_I, [_P, _P, _U64, _U64, _P]),
     "vrt_world_download_masks": (_I, [_P, _P, _P, _P, _P]),
+    "vrt_world_download_distances": (_I, [_P, _P, _P, _P]),
     "vrt_world_sync_flags": (_I, [_P, _P]),
     "vrt_world_probe": (_I, [_P, _P, _I, _P, _P]),
     "vrt_world_save": (_I, [_P, C.c_char_p, _P]),
@@ -304,6 +305,16 @@ class World:
         s = np.empty(ns, np.uint64)
         check(lib().vrt_world_download_masks(self.handle, b.ctypes.data, r.ctypes.data, s.ctypes.data, stream))
         return b, r, s
+
+    def distances(self, stream: int = 0):
+        """(brick_dir, region_dist) uint8 arrays: directed brick distances, 8 per brick
+        (byte o = octant o), and region distances."""
+        import numpy as np
+        sw, sh = (self.width + 63) // 64, (self.height + 63) // 64
+        bd = np.empty(8 * 64 * 64 * sw * sh * sw, np.uint8)
+        rd = np.empty(64 * sw * sh * sw, np.uint8)
+        check(lib().vrt_world_download_distances(self.handle, bd.ctypes.data, rd.ctypes.data, stream))
+        return bd, rd
 
     def probe(self, d_xyz: int, n: int, d_words: int, stream: int = 0):
         """Voxel words at n device (x,y,z) int32 triples; -1 outside the world."""
