@@ -458,8 +458,11 @@ int vrt_world_create(int32_t width, int32_t height, vrt_world** out) {
         return set_error(VRT_EINVAL, "world %d x %d x %d out of range", width, height, width);
     uint64_t n = (uint64_t)width * height * width;
     if (n > (1ull << 31)) return set_error(VRT_ERANGE, "world of %llu voxels exceeds 2^31", (unsigned long long)n);
+    const Layout L = make_layout(width, height);
+    if (L.n_bricks * 8 >= (1ull << 32))  // the render kernels index bricks in 32 bits
+        return set_error(VRT_ERANGE, "world %d x %d x %d: brick grid too large", width, height, width);
     vrt_world* w = new vrt_world();
-    w->L = make_layout(width, height);
+    w->L = L;
     cudaGetDevice(&w->device);
     uint64_t bytes = w->L.n_words * 4 + (w->L.n_bricks + w->L.n_regions + w->L.n_supers) * 8 + 24 * w->L.n_bricks +
                      (uint64_t)w->L.RWp * w->L.RHp * w->L.RWp + 256;
