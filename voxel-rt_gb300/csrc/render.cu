@@ -193,6 +193,7 @@ struct MaskParams {
     const uint8_t* rdist;
     int bb[6];             // solid bounding box: min x,y,z, max x,y,z (never smaller than the truth)
     int cl[6];             // tile kernel: boxes are clipped to [cl[0],cl[3]) x [cl[1],cl[4]) x [cl[2],cl[5])
+    int one, four, sixteen;  // 1, 4, 16: multipliers the compiler cannot fold (see cast_box)
     Layout L;
     const ViewDev* views;  // nviews entries (device); NULL when nviews == 1 (v0 is used)
     int nviews;
@@ -601,7 +602,7 @@ struct BoxRay {
     int kx, ky, kz;
     int ex, ey, ez;
     int sx, sy, sz;
-    int left;        // DDA iterations left, minus one: negative once the cap is used up
+    int left;        // DDA iterations left after the current one: negative on the last allowed one
     int bi;          // bit of the current cell in m (valid while m != 0)
     uint64_t m;      // voxel bits of the current brick, 0 inside an empty box
 };
@@ -660,7 +661,13 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, V3 o, V3 d, int n, 
     r.sx = s.sx; r.sy = s.sy; r.sz = s.sz;
     const int n0 = max(0, min(n, maxSteps));
     if (n0 == 0) return T_MISS;
-    r.left = n0 - 1;
+    // The bit-index updates are multiply-adds by kernel parameters equal to 1, 4 and 16.
+    // The compiler cannot turn them into plain adds, so they issue on the FMA pipe, which
+    // the intersect adds leave mostly idle, instead of the integer/logic pipe that bounds
+    // this loop.  (Doing the same for the box counters helped long empty boxes but cost
+    // more on the 1080p frame, so those stay plain adds.)
+    const int one = P.one, four = P.four, sixteen = P.sixteen;
+    r.left = n0 - 1;  // after the top-of-loop decrement: negative on the last allowed iteration
     // no box yet: the first step along any axis (even one with s == 0) triggers a lookup
     r.kx = 0; r.ky = 0; r.kz = 0;
     r.ex = s.cx + s.sx; r.ey = s.cy + s.sy; r.ez = s.cz + s.sz;
@@ -674,16 +681,17 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, V3 o, V3 d, int n, 
         if (bx) r.kx -= 1;
         if (by) r.ky -= 1;
         if (bz) r.kz -= 1;
-        const bool out = (r.kx | r.ky | r.kz) < 0;
-        bool hb = false;
+        r.left -= 1;
+        bool hb = false;  // the cell's bit, meaningful only while the step stays in the box
         if (r.m) {
-            if (bx) r.bi += r.sx;
-            if (by) r.bi += 4 * r.sy;
-            if (bz) r.bi += 16 * r.sz;
-            hb = !out && ((r.m >> (r.bi & 63)) & 1);
+            if (bx) r.bi = r.bi * one + r.sx;
+            if (by) r.bi = r.sy * four + r.bi;
+            if (bz) r.bi = r.sz * sixteen + r.bi;
+            hb = (r.m >> (r.bi & 63)) & 1;
         }
-        if (out | hb | (r.left == 0)) {
+        if (((r.kx | r.ky | r.kz | r.left) < 0) | hb) {
             const int a = bx ? 0 : (by ? 1 : 2);
+            const bool out = (r.kx | r.ky | r.kz) < 0;
             if (out) {
                 refills++;
                 const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
@@ -704,14 +712,13 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, V3 o, V3 d, int n, 
                 sgn = a == 0 ? r.sx : (a == 1 ? r.sy : r.sz);
                 break;
             }
-            if (r.left == 0) { result = T_MISS; break; }  // entered an empty box on the last iteration
+            if (r.left < 0) { result = T_MISS; break; }  // entered a box on the last iteration
         }
         if (bx) r.tx = fadd(r.tx, r.dx);
         if (by) r.ty = fadd(r.ty, r.dy);
         if (bz) r.tz = fadd(r.tz, r.dz);
-        r.left -= 1;
     }
-    steps += n0 - r.left;  // r.left counts down from n0-1 and the breaking step was not subtracted
+    steps += n0 - 1 - r.left;  // r.left = n0 - 2 - (index of the breaking iteration)
     return result;
 }
 
@@ -919,6 +926,7 @@ static int launch_mask(vrt_renderer* r, const vrt_world* w, const ViewDev* h_vie
     P.bdir = w->d_bdir;
     P.rdist = w->d_rdist;
     std::memcpy(P.bb, w->h_aabb, sizeof(P.bb));
+    P.one = 1; P.four = 4; P.sixteen = 16;
     P.L = w->L;
     P.views = nviews == 1 ? nullptr : d_views;
     P.nviews = nviews;
@@ -954,6 +962,7 @@ static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, 
     P.bdir = w->d_bdir;
     P.rdist = w->d_rdist;
     std::memcpy(P.bb, w->h_aabb, sizeof(P.bb));
+    P.one = 1; P.four = 4; P.sixteen = 16;
     P.L = w->L;
     P.views = nviews == 1 ? nullptr : d_views;
     P.nviews = nviews;
