@@ -602,14 +602,44 @@ struct BoxRay {
     int kx, ky, kz;
     int ex, ey, ez;
     int sx, sy, sz;
+    uint32_t oct;    // octant of travel: bit a set when s_a > 0
     int left;        // DDA iterations left after the current one: negative on the last allowed one
     int bi;          // bit of the current cell in m (valid while m != 0)
     uint64_t m;      // voxel bits of the current brick, 0 inside an empty box
 };
 
 __device__ __forceinline__ void set_axis(int c, int s, int lo, int hi, int& k, int& e) {
-    k = s > 0 ? hi - 1 - c : (s < 0 ? c - lo : INT_MAX);
-    e = s > 0 ? hi : (s < 0 ? lo - 1 : c);
+    // e is the first cell past the far face; k = s * (e - c) - 1 is one multiply-add,
+    // which issues on the FMA pipe rather than the integer/logic pipe
+    const int ee = s > 0 ? hi : lo - 1;
+    k = s != 0 ? s * (ee - c) - 1 : INT_MAX;
+    e = s != 0 ? ee : c;
+}
+
+// Per-octant alive ranges of a launch, one (lo, span) pair per octant and axis: a cell
+// whose coordinate c has (unsigned)(c - lo) >= span along some axis ends the ray.  Exact
+// launches hold the world, [0, dim): getVoxelIndex == -1 (fshader.glsl:123-125).
+// Inexact launches also end rays that cannot hit anything: moving + along an axis (octant
+// bit set), a cell beyond the solid box's upper face will only move further from it, so
+// the range is [0, min(dim, bb_hi + 1)); moving - or not at all, [max(0, bb_lo), dim).
+// (A ray that does not move along the axis could also end beyond the upper face; it is
+// left to walk, which costs time, not exactness.)  Kept in shared memory: three 8-byte
+// loads per lookup replace a dozen integer compares.
+__device__ __forceinline__ void fill_alive_ranges(int2* alive, const MaskParams& P, bool exact) {
+    if (threadIdx.x < 24) {
+        const int o = threadIdx.x / 3, a = threadIdx.x % 3;
+        const int dim = a == 1 ? P.L.H : P.L.W;
+        int lo = 0, span = dim;
+        if (!exact) {
+            if ((o >> a) & 1) {
+                span = max(0, min(dim, P.bb[3 + a] + 1));
+            } else {
+                lo = min(max(0, P.bb[a]), dim);
+                span = dim - lo;
+            }
+        }
+        alive[threadIdx.x] = make_int2(lo, span);
+    }
 }
 
 // The ray stands in cell c, outside any known box: load c's brick and its directed
@@ -617,27 +647,29 @@ __device__ __forceinline__ void set_axis(int c, int s, int lo, int hi, int& k, i
 // tested step by step); an empty one at directed distance d gives the cube of bricks from
 // it d-1 bricks ahead.  (Region-level cubes are not consulted: with directed brick cubes
 // they would shorten the walk by well under 1 % of lookups, less than their own cost.)
-// Returns T_LIVE, T_HIT (c is solid) or T_MISS (c is outside the world, or, for inexact
-// launches, beyond the solid box in its direction of travel).
-template <bool EXACT>
-__device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, const MaskParams& P) {
+// Returns T_LIVE, T_HIT (c is solid) or T_MISS (c is outside the alive ranges).
+__device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, const MaskParams& P,
+                                         const int2* alive) {
     const Layout& L = P.L;
-    if ((unsigned)cx >= (unsigned)L.W || (unsigned)cy >= (unsigned)L.H || (unsigned)cz >= (unsigned)L.W)
-        return T_MISS;  // getVoxelIndex == -1 (fshader.glsl:123-125)
-    if (!EXACT && beyond_solids(P, cx, cy, cz, r.sx, r.sy, r.sz)) return T_MISS;
+    const int2 ax = alive[r.oct * 3], ay = alive[r.oct * 3 + 1], az = alive[r.oct * 3 + 2];
+    if ((unsigned)(cx - ax.x) >= (unsigned)ax.y || (unsigned)(cy - ay.x) >= (unsigned)ay.y ||
+        (unsigned)(cz - az.x) >= (unsigned)az.y)
+        return T_MISS;
     const int bx = cx >> 2, by = cy >> 2, bz = cz >> 2;
     // slots in 32 bits: a world holds at most 2^31 voxels, so 8 * n_bricks < 2^32
     const uint32_t bidx = (uint32_t)bx + (uint32_t)L.BWp * ((uint32_t)by + (uint32_t)L.BHp * (uint32_t)bz);
-    const uint32_t oct = (r.sx > 0) | ((r.sy > 0) << 1) | ((r.sz > 0) << 2);
     // the two loads are independent: issue them together, wait once
     const uint64_t m = __ldg(P.bricks + bidx);
-    const int db = __ldg(P.bdir + (bidx * 8u + oct));
+    const int db = __ldg(P.bdir + (bidx * 8u + r.oct));
     const int k = m ? 0 : max(db, 1) - 1;
     // clip to the world, and for inexact launches to the solid box too: a ray that
-    // leaves the solid box along its direction of travel then ends at the next lookup
-    const int lox = max((bx - k) << 2, P.cl[0]), loy = max((by - k) << 2, P.cl[1]), loz = max((bz - k) << 2, P.cl[2]);
-    const int hix = min((bx + k + 1) << 2, P.cl[3]), hiy = min((by + k + 1) << 2, P.cl[4]),
-              hiz = min((bz + k + 1) << 2, P.cl[5]);
+    // leaves the solid box along its direction of travel then ends at the next lookup.
+    // (Multiplies by a kernel parameter equal to 4 rather than shifts: FMA pipe.)
+    const int four = P.four;
+    const int lox = max((bx - k) * four, P.cl[0]), loy = max((by - k) * four, P.cl[1]),
+              loz = max((bz - k) * four, P.cl[2]);
+    const int hix = min((bx + k + 1) * four, P.cl[3]), hiy = min((by + k + 1) * four, P.cl[4]),
+              hiz = min((bz + k + 1) * four, P.cl[5]);
     set_axis(cx, r.sx, lox, hix, r.kx, r.ex);
     set_axis(cy, r.sy, loy, hiy, r.ky, r.ey);
     set_axis(cz, r.sz, loz, hiz, r.kz, r.ez);
@@ -650,15 +682,16 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
 // shader's comparison and its one intersect add, in the shader's order; memory is read
 // only when the ray leaves its known box.  On a hit, cd / axis / sgn / cell describe the
 // last step (currDist, hitNormal, the voxel).
-template <bool EXACT>
-__device__ __forceinline__ int cast_box(const MaskParams& P, V3 o, V3 d, int n, int maxSteps, float& cd, int& axis,
-                                        int& sgn, int& steps, int32_t& hit_index, unsigned& refills) {
+__device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, V3 o, V3 d, int n, int maxSteps,
+                                        float& cd, int& axis, int& sgn, int& steps, int32_t& hit_index,
+                                        unsigned& refills) {
     RaySetup s;
     ray_setup(o, d, s);
     BoxRay r;
     r.tx = s.tx; r.ty = s.ty; r.tz = s.tz;
     r.dx = s.dx; r.dy = s.dy; r.dz = s.dz;
     r.sx = s.sx; r.sy = s.sy; r.sz = s.sz;
+    r.oct = (s.sx > 0) | ((s.sy > 0) << 1) | ((s.sz > 0) << 2);
     const int n0 = max(0, min(n, maxSteps));
     if (n0 == 0) return T_MISS;
     // The bit-index updates are multiply-adds by kernel parameters equal to 1, 4 and 16.
@@ -695,7 +728,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, V3 o, V3 d, int n, 
             if (out) {
                 refills++;
                 const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
-                const int t = enter_box<EXACT>(r, cx, cy, cz, P);
+                const int t = enter_box(r, cx, cy, cz, P, alive);
                 if (t == T_HIT) { result = T_HIT; hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz; }
                 else if (t == T_MISS) result = T_MISS;
                 else result = T_LIVE;
@@ -738,6 +771,9 @@ __device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
 // EXACT launches (any view asking for step counts) step every ray to its end.
 template <bool EXACT>
 __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_constant__ MaskParams P) {
+    __shared__ int2 alive[24];
+    fill_alive_ranges(alive, P, EXACT);
+    __syncthreads();
     const int tile = blockIdx.x;
     const ViewDev& V = view_of(P, view_of_tile(P, tile));
     const int lt = tile - V.tile_begin;
@@ -753,7 +789,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
         float cd = 0.f, c2;
         int axis = 2, sgn = 0, steps = 0, a2, s2;
         int32_t hit = -1, dummy = -1;
-        const int pr = cast_box<EXACT>(P, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit,
+        const int pr = cast_box(P, alive, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit,
                                       refills);
         res.primary_steps = steps;
         float mr = u.ambient, mg = u.ambient, mb = u.ambient;
@@ -764,7 +800,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
             const V3 hp = add3(mul3s(rd, cd), cam);
             const V3 hn = axis_normal(axis, sgn);
             const V3 toLight = norm3(sub3(V3{u.lightPos[0], u.lightPos[1], u.lightPos[2]}, hp));
-            const int sr = cast_box<EXACT>(P, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
+            const int sr = cast_box(P, alive, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
                                           u.maxSteps, c2, a2, s2, steps, dummy, refills);
             res.cast |= 1u;
             if (sr != T_HIT) {
@@ -788,7 +824,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
                     const float ld = len3(dl);
                     if (ld <= R) {
                         const V3 tl = norm3(dl);
-                        const int lr = cast_box<EXACT>(P, add3(hp, mul3s(tl, 0.001f)), tl,
+                        const int lr = cast_box(P, alive, add3(hp, mul3s(tl, 0.001f)), tl,
                                                       f2i(fadd(ld, 1.0f)), u.maxSteps, c2, a2, s2, steps, dummy,
                                                       refills);
                         res.cast |= 2u << i;
