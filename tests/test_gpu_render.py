@@ -216,3 +216,26 @@ def test_bad_arguments_fail_loudly(cuda, small):
     u.maxSteps = -1
     with pytest.raises(vrt.VrtError):
         gpu_render(w, u, 8, 8)
+
+
+@pytest.mark.parametrize("radius, intensity, limit", [(6.0, 1.0, 1.25), (16.0, 3.0, 1.3), (3.0, 2.0, 1.25)])
+def test_local_light_radius_and_overbright(cuda, oracle, radius, intensity, limit):
+    """Lights near the surface with small radii: neighbouring pixels see different lights
+    in range, and with strong lights the overbright clamp falls after different lights."""
+    W, H, seed = 128, 64, 31
+    words = vrt.terrain_generate(W, H, seed, 0)
+    rng = scenes.SplitMix64(seed)
+    u = scenes.base_uniforms(192, 128, 256, 70.0, radius)
+    scenes.set_lights(u, scenes.place_lights(rng, W, seed, 16), intensity)
+    scenes.aim(u, scenes.surface_camera(rng, W, seed, above=12.0), rng.uniform(0.0, 360.0), -35.0)
+    u.lightPos[:] = scenes.sun_position(rng, W, H)
+    u.maxOverbright = limit
+    u.aspectRatio = 192 / 128
+    o = oracle.render(words, W, H, u, 192, 128)
+    assert ((o["cast"] >> 1) != 0).sum() > 40
+    w = make_world(words, W, H)
+    for k in KERNELS:
+        assert_same_frame(o, gpu_render(w, u, 192, 128, kernel=k))
+        g = gpu_render(w, u, 192, 128, kernel=k, debug=False)  # inexact launch: images and ray counts
+        assert np.array_equal(o["rgba"], g["rgba"])
+        assert int(g["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"]

@@ -103,6 +103,29 @@ def test_overbright_break_stops_casting(oracle):
     assert casts.max() < 17
 
 
+def test_overbright_clamp_position_follows_the_shader_loop(oracle):
+    # fshader.glsl:159-164: the test runs before each of the 16 iterations, so a multiplier
+    # pushed over the limit by light i is clamped only if an iteration i+1 exists
+    def run(idx, diffuse=None):
+        u = down_uniforms(9, 7)
+        for i in idx:
+            u.localLights[i][:] = [6.0 + 0.1 * i, 3.0, 7.0, 4.0]
+        if diffuse is not None:
+            u.diffuse = diffuse
+        out = oracle.render(floor_world(), S, S, u, 9, 7)
+        h = out["hit"] >= 0
+        assert h.sum() > 20
+        return out["shade"][h], out["cast"][h]
+    shade, cast = run((3, 9, 15))
+    assert (shade == np.float32(1.25)).all() and (cast == 1 | (2 << 3)).all()  # 9 and 15 never cast
+    shade, cast = run((14,))
+    assert (shade == np.float32(1.25)).all() and (cast == 1 | (2 << 14)).all()
+    shade, cast = run((15,))
+    assert (shade > np.float32(1.25)).all() and (cast == 1 | (2 << 15)).all()  # no test after light 15
+    shade, cast = run((), diffuse=2.0)
+    assert (shade == np.float32(1.25)).all() and (cast == 1).all()
+
+
 def test_inactive_and_far_lights_are_not_cast(oracle):
     u = down_uniforms()
     u.localLights[0][:] = [-1.0, 3.0, 7.0, 1.0]    # x < 0: inactive (fshader.glsl:167)
@@ -147,6 +170,17 @@ def kat_scenes():
     for i in range(16):
         u.localLights[i][:] = [6.0 + 0.1 * i, 3.0, 7.0, 1.0]
     scenes.append(("overbright", floor_world(), u, 9, 7))
+    # the overbright clamp with sparse active lights: after light 3 it falls before light 9
+    # (only 3 is cast); after light 14 the shader's loop still tests at i = 15 and clamps;
+    # after light 15 there is no test left and the multiplier stays above the limit
+    for name, idx in (("overbright-sparse", (3, 9, 15)), ("overbright-14", (14,)), ("overbright-15", (15,))):
+        u = down_uniforms(9, 7)
+        for i in idx:
+            u.localLights[i][:] = [6.0 + 0.1 * i, 3.0, 7.0, 4.0]
+        scenes.append((name, floor_world(), u, 9, 7))
+    u = down_uniforms(9, 7)
+    u.diffuse = 2.0  # the global light alone passes the limit: clamped before light 0
+    scenes.append(("overbright-global", floor_world(), u, 9, 7))
     u = down_uniforms(8, 8)
     u.localLights[0][:] = [-1.0, 3.0, 7.0, 1.0]
     u.localLights[2][:] = [6.0, 3.0, 7.0, 0.5]

@@ -766,6 +766,33 @@ __device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
     return lo;
 }
 
+// The local lights that may be in range of some lane of the warp, as a warp-uniform bit
+// mask: lane l < 16 tests light l's cube of half-size R1 + 1 against the integer
+// bounding box of the warp's hit points (every lane must call this).  A light a lane
+// would accept (every |L - hitPos| component within R1, fshader.glsl:168-171 with the
+// pre-reject above) lies within that box grown by R1 + 1, so no candidate is lost; an
+// inactive light (a coordinate < 0, :167) never is one.
+__device__ __forceinline__ unsigned warp_light_candidates(const vrt_uniforms& u, bool lit, V3 hp) {
+    const unsigned full = 0xffffffffu;
+    const int x0 = __reduce_min_sync(full, lit ? (int)floorf(hp.x) : INT_MAX);
+    const int y0 = __reduce_min_sync(full, lit ? (int)floorf(hp.y) : INT_MAX);
+    const int z0 = __reduce_min_sync(full, lit ? (int)floorf(hp.z) : INT_MAX);
+    const int x1 = __reduce_max_sync(full, lit ? (int)floorf(hp.x) + 1 : INT_MIN);
+    const int y1 = __reduce_max_sync(full, lit ? (int)floorf(hp.y) + 1 : INT_MIN);
+    const int z1 = __reduce_max_sync(full, lit ? (int)floorf(hp.z) + 1 : INT_MIN);
+    const int lane = threadIdx.x & 31;
+    bool c = false;
+    if (x0 != INT_MAX && lane < VRT_MAX_LOCAL_LIGHTS) {
+        const float* L = u.localLights[lane];
+        if (L[0] >= 0 && L[1] >= 0 && L[2] >= 0) {
+            const float g = fabsf(u.localLightDist) * 1.0009765625f + 2.0f;
+            c = L[0] + g >= (float)x0 && L[0] - g <= (float)x1 && L[1] + g >= (float)y0 && L[1] - g <= (float)y1 &&
+                L[2] + g >= (float)z0 && L[2] - g <= (float)z1;
+        }
+    }
+    return __ballot_sync(full, c);
+}
+
 // One CTA per ray tile (tile_w x tile_h pixels, tile_w*tile_h == blockDim.x) over the tile
 // space of every view of the launch: a single frame, or a batch of cameras of any sizes.
 // EXACT launches (any view asking for step counts) step every ray to its end.
@@ -782,65 +809,94 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
     const bool valid = px < V.width && py < V.height;
     PixelResult res{};
     unsigned refills = 0;
+    const vrt_uniforms& u = V.u;
+    const V3 cam{u.camPos[0], u.camPos[1], u.camPos[2]};
+    V3 rd{0.f, 0.f, 0.f};
+    float cd = 0.f, c2 = 0.f;
+    int axis = 2, sgn = 0, steps = 0, a2 = 0, s2 = 0;
+    int32_t hit = -1, dummy = -1;
+    int pr = T_MISS;
     if (valid) {
-        const vrt_uniforms& u = V.u;
-        const V3 cam{u.camPos[0], u.camPos[1], u.camPos[2]};
-        const V3 rd = primary_dir(u, px, py, V.width, V.height);
-        float cd = 0.f, c2;
-        int axis = 2, sgn = 0, steps = 0, a2, s2;
-        int32_t hit = -1, dummy = -1;
-        const int pr = cast_box(P, alive, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit,
-                                      refills);
+        rd = primary_dir(u, px, py, V.width, V.height);
+        pr = cast_box(P, alive, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit, refills);
         res.primary_steps = steps;
+    }
+    const bool lit = valid && pr == T_HIT && u.viewDepthField != 1;
+    const V3 hp = lit ? add3(mul3s(rd, cd), cam) : V3{0.f, 0.f, 0.f};
+    const unsigned cand = warp_light_candidates(u, lit, hp);
+    if (valid) {
         float mr = u.ambient, mg = u.ambient, mb = u.ambient;
         int32_t word = 0;
         if (u.viewDepthField == 1) {
             mr = mg = mb = fdiv((float)steps, 100.0f);
         } else if (pr == T_HIT) {
-            const V3 hp = add3(mul3s(rd, cd), cam);
             const V3 hn = axis_normal(axis, sgn);
-            const V3 toLight = norm3(sub3(V3{u.lightPos[0], u.lightPos[1], u.lightPos[2]}, hp));
-            const int sr = cast_box(P, alive, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps,
-                                          u.maxSteps, c2, a2, s2, steps, dummy, refills);
-            res.cast |= 1u;
-            if (sr != T_HIT) {
-                const float c = fmul(u.diffuse, fmax0(dot3(hn, toLight)));
-                mr = fadd(mr, c); mg = fadd(mg, c); mb = fadd(mb, c);
-            } else {
-                res.occ |= 1u;
-            }
-            // R1 = |R|(1 + 2^-10) + 1 exceeds R by more than the rounding of any computed length
             const float ob = u.maxOverbright, R = u.localLightDist;
+            // R1 = |R|(1 + 2^-10) + 1 exceeds R by more than the rounding of any computed length
             const float R1 = fadd(fmul(fabsf(R), 1.0009765625f), 1.0f);
-            for (int i = 0; i < VRT_MAX_LOCAL_LIGHTS; i++) {
-                if (mr >= ob && mg >= ob && mb >= ob) {
-                    mr = mg = mb = ob;
-                    break;
-                } else if (u.localLights[i][0] >= 0 && u.localLights[i][1] >= 0 && u.localLights[i][2] >= 0) {
-                    const V3 Lp{u.localLights[i][0], u.localLights[i][1], u.localLights[i][2]};
-                    const V3 dl = sub3(Lp, hp);
+            // The shadow rays in the shader's order, through one traversal call site: j = -1
+            // is the global light (fshader.glsl:147-156), then the warp's candidate local
+            // lights in ascending order (:159-181).  The shader tests for overbright before
+            // every local light; the colour changes only at lights that are cast, so testing
+            // before each candidate, and once more after the last candidate if the shader's
+            // loop had iterations left, gives the same clamp.
+            unsigned todo = cand;
+            int last = -1;
+            bool clamped = false;
+            for (int j = -1;;) {
+                V3 dir{0.f, 0.f, 0.f};
+                int n = 0;
+                float ld = 0.f;
+                bool cast = true;
+                if (j < 0) {
+                    dir = norm3(sub3(V3{u.lightPos[0], u.lightPos[1], u.lightPos[2]}, hp));
+                    n = u.maxSteps;
+                } else {
+                    if (mr >= ob && mg >= ob && mb >= ob) {
+                        mr = mg = mb = ob;
+                        clamped = true;
+                        break;
+                    }
+                    const float* Lj = u.localLights[j];
+                    const V3 dl = sub3(V3{Lj[0], Lj[1], Lj[2]}, hp);
                     // a component beyond R1 puts the computed length beyond R too: out of range
-                    if (fabsf(dl.x) > R1 || fabsf(dl.y) > R1 || fabsf(dl.z) > R1) continue;
-                    const float ld = len3(dl);
-                    if (ld <= R) {
-                        const V3 tl = norm3(dl);
-                        const int lr = cast_box(P, alive, add3(hp, mul3s(tl, 0.001f)), tl,
-                                                      f2i(fadd(ld, 1.0f)), u.maxSteps, c2, a2, s2, steps, dummy,
-                                                      refills);
-                        res.cast |= 2u << i;
-                        if (lr != T_HIT) {
-                            const float nl = fmax0(dot3(hn, tl));
-                            const float fall = fdiv(fsub(R, ld), R);
-                            const float a = u.localLights[i][3];
-                            mr = fadd(mr, fmul(fmul(fmul(a, u.localLightColor[i][0]), nl), fall));
-                            mg = fadd(mg, fmul(fmul(fmul(a, u.localLightColor[i][1]), nl), fall));
-                            mb = fadd(mb, fmul(fmul(fmul(a, u.localLightColor[i][2]), nl), fall));
+                    cast = !(fabsf(dl.x) > R1 || fabsf(dl.y) > R1 || fabsf(dl.z) > R1);
+                    if (cast) {
+                        ld = len3(dl);
+                        cast = ld <= R;
+                    }
+                    if (cast) {
+                        dir = norm3(dl);
+                        n = f2i(fadd(ld, 1.0f));
+                    }
+                }
+                if (cast) {
+                    const int sr = cast_box(P, alive, add3(hp, mul3s(dir, 0.001f)), dir, n, u.maxSteps, c2, a2, s2,
+                                            steps, dummy, refills);
+                    const unsigned bit = 1u << (j + 1);
+                    res.cast |= bit;
+                    if (sr == T_HIT) {
+                        res.occ |= bit;
+                    } else {
+                        const float nl = fmax0(dot3(hn, dir));
+                        if (j < 0) {
+                            const float c = fmul(u.diffuse, nl);
+                            mr = fadd(mr, c); mg = fadd(mg, c); mb = fadd(mb, c);
                         } else {
-                            res.occ |= 2u << i;
+                            const float fall = fdiv(fsub(R, ld), R);
+                            const float a = u.localLights[j][3];
+                            mr = fadd(mr, fmul(fmul(fmul(a, u.localLightColor[j][0]), nl), fall));
+                            mg = fadd(mg, fmul(fmul(fmul(a, u.localLightColor[j][1]), nl), fall));
+                            mb = fadd(mb, fmul(fmul(fmul(a, u.localLightColor[j][2]), nl), fall));
                         }
                     }
                 }
+                if (!todo) break;
+                j = __ffs(todo) - 1;
+                todo &= todo - 1;
+                last = j;
             }
+            if (!clamped && last < VRT_MAX_LOCAL_LIGHTS - 1 && mr >= ob && mg >= ob && mb >= ob) mr = mg = mb = ob;
             word = __ldg(P.words + hit);
         }
         res.hit = pr == T_HIT ? hit : -1;
