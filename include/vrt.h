@@ -115,8 +115,11 @@ typedef struct vrt_render_opts {
     int32_t kernel;          /* VRT_KERNEL_*                                        */
     int32_t tile_w, tile_h;  /* ray tile (0 = kernel default: 8x16 tile kernel, 8x4 persistent) */
     int32_t refill_min;      /* persistent kernel: lanes parked before a slow phase (0 = default) */
-    int32_t blocks_per_sm;   /* resident CTAs per SM the kernel is built for (persistent: 3-4, tile: 8, 10, 12) */
+    int32_t blocks_per_sm;   /* persistent kernel: resident CTAs per SM it is built for (3 or 4) */
     int32_t exact_steps;     /* 1: count every DDA iteration of the shader, no early miss */
+    int32_t host_bands;      /* vrt_render_to_host with the tile kernel: the frame is rendered in this many
+                                bands of rows, each band's copy to the host overlapping the next band's
+                                render (0 = automatic, 1 = render then copy) */
 } vrt_render_opts;
 
 typedef struct vrt_world vrt_world;
@@ -236,8 +239,10 @@ int vrt_renderer_destroy(vrt_renderer* r);
 int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
                int32_t height, uint8_t* d_rgba, const vrt_debug_out* dbg, uint64_t* d_stats,
                const vrt_render_opts* opts, void* stream);
-/* vrt_render into the renderer's staging buffer, then copy the image to host memory
- * (pinned for overlap).  Waits for the stream before returning. */
+/* vrt_render into the renderer's staging buffer and copy the image to host memory (pinned,
+ * for the copies to run asynchronously).  With the tile kernel the frame is rendered in bands
+ * of rows (vrt_render_opts.host_bands) and each band's copy runs on the renderer's copy
+ * stream while the next band renders.  Waits for the image before returning. */
 int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
                        int32_t height, uint8_t* host_rgba, const vrt_render_opts* opts, void* stream);
 

@@ -204,6 +204,27 @@ def test_render_to_host(cuda, small):
     assert np.array_equal(host.reshape(sc.height, sc.width, 4), g["rgba"])
 
 
+@pytest.mark.parametrize("bands", [0, 1, 2, 3, 5, 8, 64])
+def test_render_to_host_in_bands(cuda, small, bands):
+    """The banded host render (each band's copy overlapping the next band's render) gives
+    the plain render's image, also when the last ray tile row is partly outside the image."""
+    sc = small
+    width, height = 200, 250
+    u = sc.uniforms
+    u.aspectRatio = width / height
+    w = make_world(sc.words, sc.W, sc.H)
+    g = gpu_render(w, u, width, height, kernel=vrt.KERNEL_MASK_PIXEL)
+    r = vrt.Renderer()
+    import torch
+    host = torch.zeros(width * height * 4, dtype=torch.uint8, pin_memory=True)
+    o = vrt.RenderOpts()
+    o.host_bands = bands
+    for _ in range(2):  # the renderer's copy stream and events are reused
+        host.zero_()
+        r.render_to_host(w, u, width, height, host.data_ptr(), o)
+        assert np.array_equal(host.numpy().reshape(height, width, 4), g["rgba"])
+
+
 def test_bad_arguments_fail_loudly(cuda, small):
     sc = small
     w = make_world(sc.words, sc.W, sc.H)

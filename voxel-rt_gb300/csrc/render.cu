@@ -193,6 +193,7 @@ struct MaskParams {
     const uint8_t* rdist;
     int bb[6];             // solid bounding box: min x,y,z, max x,y,z (never smaller than the truth)
     int cl[6];             // tile kernel: boxes are clipped to [cl[0],cl[3]) x [cl[1],cl[4]) x [cl[2],cl[5])
+    int tile0;             // tile kernel: the launch covers tiles [tile0, tile0 + gridDim.x)
     int one, four, sixteen;  // 1, 4, 16: multipliers the compiler cannot fold (see cast_box)
     Layout L;
     const ViewDev* views;  // nviews entries (device); NULL when nviews == 1 (v0 is used)
@@ -801,7 +802,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
     __shared__ int2 alive[24];
     fill_alive_ranges(alive, P, EXACT);
     __syncthreads();
-    const int tile = blockIdx.x;
+    const int tile = (int)blockIdx.x + P.tile0;
     const ViewDev& V = view_of(P, view_of_tile(P, tile));
     const int lt = tile - V.tile_begin;
     const int px = (lt % V.tiles_x) * V.tile_w + (int)threadIdx.x % V.tile_w;
@@ -955,6 +956,11 @@ struct vrt_renderer {
     unsigned int* d_counter = nullptr;
     uint8_t* d_staging = nullptr;
     size_t staging_bytes = 0;
+    cudaStream_t copy_stream = nullptr;   // vrt_render_to_host: band copies
+    cudaStream_t band_stream[8] = {};     // vrt_render_to_host: one render stream per band
+    cudaEvent_t start = nullptr;          // the caller's stream reached the render
+    cudaEvent_t band_done[8] = {};        // a band's render finished
+    cudaEvent_t copies_done = nullptr;    // the last band copy finished (copy stream)
 };
 
 struct vrt_batch_graph {
@@ -1046,7 +1052,7 @@ static int launch_mask(vrt_renderer* r, const vrt_world* w, const ViewDev* h_vie
 
 // Tile kernel launch over the views' tile space (1 view: h_views[0] as a parameter).
 static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, int total_tiles,
-                        const ViewDev* d_views, int threads, cudaStream_t s) {
+                        const ViewDev* d_views, int threads, cudaStream_t s, int tile0 = 0, int ntiles = -1) {
     MaskParams P;
     std::memset(&P, 0, sizeof(P));
     P.words = w->d_words;
@@ -1068,7 +1074,9 @@ static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, 
         P.cl[3 + a] = exact ? dims[a] : std::min(dims[a], std::max(P.bb[3 + a] + 1, P.cl[a]));
     }
     auto kern = exact ? render_tiles_kernel<true> : render_tiles_kernel<false>;
-    if (total_tiles > 0) kern<<<total_tiles, threads, 0, s>>>(P);
+    P.tile0 = tile0;
+    if (ntiles < 0) ntiles = total_tiles - tile0;
+    if (ntiles > 0) kern<<<ntiles, threads, 0, s>>>(P);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
@@ -1128,6 +1136,13 @@ int vrt_renderer_destroy(vrt_renderer* r) {
     cudaFree(r->d_views);
     cudaFree(r->d_counter);
     cudaFree(r->d_staging);
+    if (r->copy_stream) cudaStreamDestroy(r->copy_stream);
+    for (cudaStream_t b : r->band_stream)
+        if (b) cudaStreamDestroy(b);
+    for (cudaEvent_t e : r->band_done)
+        if (e) cudaEventDestroy(e);
+    if (r->start) cudaEventDestroy(r->start);
+    if (r->copies_done) cudaEventDestroy(r->copies_done);
     delete r;
     return VRT_OK;
 }
@@ -1175,11 +1190,24 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
     return launch_mask(r, w, &v, 1, tiles_of(width, height, t), t, nullptr, r->d_counter, S(stream));
 }
 
+// The streams and events of the banded host render, made on first use.
+static int ensure_band_resources(vrt_renderer* r) {
+    if (r->copy_stream) return VRT_OK;
+    for (cudaStream_t& b : r->band_stream) VRT_CUDA(cudaStreamCreateWithFlags(&b, cudaStreamNonBlocking));
+    for (cudaEvent_t& e : r->band_done) VRT_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
+    VRT_CUDA(cudaEventCreateWithFlags(&r->start, cudaEventDisableTiming));
+    VRT_CUDA(cudaEventCreateWithFlags(&r->copies_done, cudaEventDisableTiming));
+    VRT_CUDA(cudaStreamCreateWithFlags(&r->copy_stream, cudaStreamNonBlocking));  // last: marks the set made
+    return VRT_OK;
+}
+
 int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width, int32_t height,
                        uint8_t* host_rgba, const vrt_render_opts* opts, void* stream) {
-    if (!r || !host_rgba) return set_error(VRT_EINVAL, "NULL renderer or image");
+    if (!r || !w || !host_rgba) return set_error(VRT_EINVAL, "NULL renderer, world or image");
     if (width < 1 || height < 1 || width > 32768 || height > 32768)
         return set_error(VRT_EINVAL, "image %d x %d out of range", width, height);
+    int st = check_uniforms(u);
+    if (st) return st;
     size_t bytes = (size_t)width * height * 4;
     if (bytes > r->staging_bytes) {
         cudaFree(r->d_staging);
@@ -1189,10 +1217,53 @@ int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* 
         if (e != cudaSuccess) return set_error(VRT_ENOMEM, "staging image: %s", cudaGetErrorString(e));
         r->staging_bytes = bytes;
     }
-    int st = vrt_render(r, w, u, width, height, r->d_staging, nullptr, nullptr, opts, stream);
+    const cudaStream_t s = S(stream);
+    int kernel = opts ? opts->kernel : VRT_KERNEL_AUTO;
+    if (kernel == VRT_KERNEL_AUTO && !w->has_depth_field) kernel = VRT_KERNEL_MASK_PIXEL;
+    int bands = 1;
+    Tuning t{};
+    if (kernel == VRT_KERNEL_MASK_PIXEL && !w->has_depth_field) {
+        st = tile_tuning(opts, &t);
+        if (st) return st;
+        const int tiles_y = (height + t.tile_h - 1) / t.tile_h;
+        // automatic: one band per 128 rows, up to 8, so that only the last band's copy is
+        // exposed (1080p: 8 bands, 0.292 -> 0.265 ms per frame to pinned host memory)
+        bands = opts && opts->host_bands > 0 ? opts->host_bands : std::max(1, std::min(8, height / 128));
+        bands = std::max(1, std::min({bands, tiles_y, 8}));
+    }
+    if (bands == 1) {
+        st = vrt_render(r, w, u, width, height, r->d_staging, nullptr, nullptr, opts, stream);
+        if (st) return st;
+        VRT_CUDA(cudaMemcpyAsync(host_rgba, r->d_staging, bytes, cudaMemcpyDeviceToHost, s));
+        VRT_CUDA(cudaStreamSynchronize(s));
+        return VRT_OK;
+    }
+    st = ensure_band_resources(r);
     if (st) return st;
-    VRT_CUDA(cudaMemcpyAsync(host_rgba, r->d_staging, bytes, cudaMemcpyDeviceToHost, S(stream)));
-    VRT_CUDA(cudaStreamSynchronize(S(stream)));
+    ViewDev v;
+    fill_view(v, *u, width, height, r->d_staging, nullptr, nullptr, t, 0);
+    const int tiles_x = v.tiles_x, tiles_y = (height + t.tile_h - 1) / t.tile_h;
+    const int total = tiles_x * tiles_y;
+    const size_t row_bytes = (size_t)width * 4;
+    // Each band renders on its own stream, with no order among the bands: the launches run
+    // back to back like one grid (a band's last wave overlaps the next band's first), and
+    // each band's copy starts as soon as that band is done.
+    VRT_CUDA(cudaEventRecord(r->start, s));
+    for (int b = 0; b < bands; b++) {
+        const int r0 = (int)((int64_t)tiles_y * b / bands), r1 = (int)((int64_t)tiles_y * (b + 1) / bands);
+        VRT_CUDA(cudaStreamWaitEvent(r->band_stream[b], r->start, 0));
+        st = launch_tiles(w, &v, 1, total, nullptr, t.tile_w * t.tile_h, r->band_stream[b], r0 * tiles_x,
+                          (r1 - r0) * tiles_x);
+        if (st) return st;
+        VRT_CUDA(cudaEventRecord(r->band_done[b], r->band_stream[b]));
+        VRT_CUDA(cudaStreamWaitEvent(r->copy_stream, r->band_done[b], 0));
+        const int y0 = r0 * t.tile_h, y1 = std::min(height, r1 * t.tile_h);
+        VRT_CUDA(cudaMemcpyAsync(host_rgba + (size_t)y0 * row_bytes, r->d_staging + (size_t)y0 * row_bytes,
+                                 (size_t)(y1 - y0) * row_bytes, cudaMemcpyDeviceToHost, r->copy_stream));
+    }
+    VRT_CUDA(cudaEventRecord(r->copies_done, r->copy_stream));
+    VRT_CUDA(cudaStreamWaitEvent(s, r->copies_done, 0));  // later work on the stream follows the copies
+    VRT_CUDA(cudaEventSynchronize(r->copies_done));
     return VRT_OK;
 }
 

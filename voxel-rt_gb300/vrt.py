@@ -78,6 +78,7 @@ class RenderOpts(C.Structure):
         ("refill_min", C.c_int32),
         ("blocks_per_sm", C.c_int32),
         ("exact_steps", C.c_int32),
+        ("host_bands", C.c_int32),
     ]
 
 
