@@ -245,6 +245,11 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
  * stream while the next band renders.  Waits for the image before returning. */
 int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
                        int32_t height, uint8_t* host_rgba, const vrt_render_opts* opts, void* stream);
+/* Page-locked host memory for images (cudaMallocHost), for callers without CUDA headers:
+ * copies into it run asynchronously, which vrt_render_to_host's bands need to overlap the
+ * render.  No counterpart in the reference.  vrt_host_free(NULL) is a no-op. */
+int vrt_host_alloc(size_t bytes, void** out);
+int vrt_host_free(void* p);
 
 /* One camera of a batch. */
 typedef struct vrt_view {

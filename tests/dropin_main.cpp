@@ -28,13 +28,13 @@ int main(int argc, char** argv) {
     placeLocalLight(camPos.x, camPos.y - 1.5f, camPos.z, 0.5f);  // the T key, controls.cpp:46-49
     updateUniforms();
     const uint8_t* f0 = drawFrame();
-    if (!dump(out + "/frame0.rgba", f0, (size_t)screenWidth * screenHeight * 4)) return 2;
+    if (!f0 || !dump(out + "/frame0.rgba", f0, (size_t)screenWidth * screenHeight * 4)) return 2;
     // doDestroy (removeSphere(center, 7)) aimed at the grass surface 30 voxels ahead
     const ivec3 c{(int)camPos.x, 36, (int)(camPos.z + 30.0f)};
     removeSphere(c, 7);
     updateUniforms();
     const uint8_t* f1 = drawFrame();
-    if (!dump(out + "/frame1.rgba", f1, (size_t)screenWidth * screenHeight * 4)) return 2;
+    if (!f1 || !dump(out + "/frame1.rgba", f1, (size_t)screenWidth * screenHeight * 4)) return 2;
     if (!dump(out + "/world1.i32", voxels, (size_t)VOXELS_WIDTH * VOXELS_HEIGHT * VOXELS_WIDTH * 4)) return 2;
     float params[11] = {camPos.x, camPos.y, camPos.z, lightPos.x, lightPos.y, lightPos.z, aspectRatio,
                         (float)RENDER_DIST, (float)c.x, (float)c.y, (float)c.z};

@@ -260,3 +260,33 @@ def test_local_light_radius_and_overbright(cuda, oracle, radius, intensity, limi
         g = gpu_render(w, u, 192, 128, kernel=k, debug=False)  # inexact launch: images and ray counts
         assert np.array_equal(o["rgba"], g["rgba"])
         assert int(g["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"]
+
+
+def test_host_alloc_and_pageable_bands(cuda, small):
+    """vrt_host_alloc gives page-locked memory the banded copies run into; a pageable
+    buffer (whose copies block the caller) gets the same image."""
+    import ctypes as C
+    sc = small
+    width, height = 160, 300
+    u = sc.uniforms
+    u.aspectRatio = width / height
+    w = make_world(sc.words, sc.W, sc.H)
+    g = gpu_render(w, u, width, height, kernel=vrt.KERNEL_MASK_PIXEL)
+    r = vrt.Renderer()
+    o = vrt.RenderOpts()
+    o.host_bands = 4
+    p = C.c_void_p()
+    vrt.check(vrt.lib().vrt_host_alloc(width * height * 4, C.byref(p)))
+    assert p.value
+    try:
+        pinned = np.ctypeslib.as_array((C.c_uint8 * (width * height * 4)).from_address(p.value))
+        r.render_to_host(w, u, width, height, p.value, o)
+        assert np.array_equal(pinned.reshape(height, width, 4), g["rgba"])
+    finally:
+        vrt.check(vrt.lib().vrt_host_free(p))
+    pageable = np.zeros(width * height * 4, np.uint8)
+    r.render_to_host(w, u, width, height, pageable.ctypes.data, o)
+    assert np.array_equal(pageable.reshape(height, width, 4), g["rgba"])
+    q = C.c_void_p(1)
+    vrt.check(vrt.lib().vrt_host_alloc(0, C.byref(q)))
+    assert not q.value and vrt.lib().vrt_host_free(None) == 0

@@ -1190,6 +1190,24 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
     return launch_mask(r, w, &v, 1, tiles_of(width, height, t), t, nullptr, r->d_counter, S(stream));
 }
 
+int vrt_host_alloc(size_t bytes, void** out) {
+    if (!out) return set_error(VRT_EINVAL, "out is NULL");
+    *out = nullptr;
+    if (bytes == 0) return VRT_OK;
+    cudaError_t e = cudaMallocHost(out, bytes);
+    if (e != cudaSuccess) {
+        *out = nullptr;
+        return e == cudaErrorMemoryAllocation ? set_error(VRT_ENOMEM, "pinned host buffer of %zu bytes", bytes)
+                                              : cuda_error(e, "cudaMallocHost");
+    }
+    return VRT_OK;
+}
+
+int vrt_host_free(void* p) {
+    if (p) VRT_CUDA(cudaFreeHost(p));
+    return VRT_OK;
+}
+
 // The streams and events of the banded host render, made on first use.
 static int ensure_band_resources(vrt_renderer* r) {
     if (r->copy_stream) return VRT_OK;
@@ -1247,7 +1265,8 @@ int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* 
     const size_t row_bytes = (size_t)width * 4;
     // Each band renders on its own stream, with no order among the bands: the launches run
     // back to back like one grid (a band's last wave overlaps the next band's first), and
-    // each band's copy starts as soon as that band is done.
+    // each band's copy starts as soon as that band is done.  Every band is queued before
+    // the first copy, because a copy to pageable host memory blocks the calling thread.
     VRT_CUDA(cudaEventRecord(r->start, s));
     for (int b = 0; b < bands; b++) {
         const int r0 = (int)((int64_t)tiles_y * b / bands), r1 = (int)((int64_t)tiles_y * (b + 1) / bands);
@@ -1256,6 +1275,9 @@ int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* 
                           (r1 - r0) * tiles_x);
         if (st) return st;
         VRT_CUDA(cudaEventRecord(r->band_done[b], r->band_stream[b]));
+    }
+    for (int b = 0; b < bands; b++) {
+        const int r0 = (int)((int64_t)tiles_y * b / bands), r1 = (int)((int64_t)tiles_y * (b + 1) / bands);
         VRT_CUDA(cudaStreamWaitEvent(r->copy_stream, r->band_done[b], 0));
         const int y0 = r0 * t.tile_h, y1 = std::min(height, r1 * t.tile_h);
         VRT_CUDA(cudaMemcpyAsync(host_rgba + (size_t)y0 * row_bytes, r->d_staging + (size_t)y0 * row_bytes,

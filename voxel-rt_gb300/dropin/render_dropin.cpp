@@ -27,7 +27,8 @@ vrt_world* g_world = nullptr;
 vrt_renderer* g_renderer = nullptr;
 vrt_uniforms g_u;
 std::vector<int32_t> g_mirror;
-std::vector<uint8_t> g_frame;
+uint8_t* g_frame = nullptr;  // page-locked (vrt_host_alloc), so the frame's band copies overlap the render
+size_t g_frame_bytes = 0;
 int g_status = 0;
 
 inline void note(int st) {
@@ -61,6 +62,9 @@ int initRender(int width, int height, int with_reference_world) {
 }
 
 void shutdownRender() {
+    vrt_host_free(g_frame);
+    g_frame = nullptr;
+    g_frame_bytes = 0;
     vrt_renderer_destroy(g_renderer);
     vrt_world_destroy(g_world);
     g_renderer = nullptr;
@@ -180,9 +184,20 @@ void reshape(int width, int height) {
 }
 
 const uint8_t* drawFrame() {
-    g_frame.resize((size_t)screenWidth * screenHeight * 4);
-    note(vrt_render_to_host(g_renderer, g_world, &g_u, screenWidth, screenHeight, g_frame.data(), nullptr, nullptr));
-    return g_frame.data();
+    const size_t bytes = (size_t)screenWidth * screenHeight * 4;
+    if (bytes > g_frame_bytes) {
+        vrt_host_free(g_frame);
+        g_frame = nullptr;
+        g_frame_bytes = 0;
+        void* p = nullptr;
+        const int st = vrt_host_alloc(bytes, &p);
+        note(st);
+        if (st) return nullptr;
+        g_frame = static_cast<uint8_t*>(p);
+        g_frame_bytes = bytes;
+    }
+    note(vrt_render_to_host(g_renderer, g_world, &g_u, screenWidth, screenHeight, g_frame, nullptr, nullptr));
+    return g_frame;
 }
 
 }  // namespace vrtdrop

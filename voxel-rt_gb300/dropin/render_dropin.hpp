@@ -59,7 +59,8 @@ void placeLocalLight(float x, float y, float z, float diffuse);  // render.cpp:3
 void initLocalLights();                                 // render.cpp:304-311
 
 // glDrawArrays(GL_TRIANGLES, 0, 6) (main.cpp:59): one frame of screenWidth x
-// screenHeight into the returned host RGBA8 buffer (valid until the next call).
+// screenHeight into the returned host RGBA8 buffer (page-locked; valid until the next
+// call or shutdownRender; NULL if it could not be allocated).
 const uint8_t* drawFrame();
 
 int vrtStatus();                 // status of the last failing call, 0 if none

@@ -181,6 +181,8 @@ SIGNATURES = {
     "vrt_render": (_I, [_P, _P, C.POINTER(Uniforms), _I, _I, _P, C.POINTER(DebugOut), _P,
                         C.POINTER(RenderOpts), _P]),
     "vrt_render_to_host": (_I, [_P, _P, C.POINTER(Uniforms), _I, _I, _P, C.POINTER(RenderOpts), _P]),
+    "vrt_host_alloc": (_I, [C.c_size_t, C.POINTER(_P)]),
+    "vrt_host_free": (_I, [_P]),
     "vrt_render_batch": (_I, [_P, C.POINTER(View), _I, C.POINTER(RenderOpts), _P]),
     "vrt_render_batch_noalloc": (_I, [C.POINTER(View), _I, C.POINTER(RenderOpts), _P]),
     "vrt_batch_graph_create": (_I, [_P, C.POINTER(View), _I, C.POINTER(RenderOpts), _P, C.POINTER(_P)]),
