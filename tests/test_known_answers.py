@@ -79,6 +79,17 @@ def floor_world():
     return world([(x, 0, z) for x in range(S) for z in range(S)])
 
 
+def palette_floor_world():
+    """The floor with voxel (x, 0, z) coloured by i = x + 16z: red i, green 255 - i, blue
+    37i mod 256, so every 8-bit channel value appears (the shader's ch / 255 scale)."""
+    w = np.full(S * S * S, -1, np.int32)
+    for z in range(S):
+        for x in range(S):
+            i = x + 16 * z
+            w[idx(x, 0, z)] = 0x01000000 | (i << 16) | ((255 - i) << 8) | ((i * 37) & 255)
+    return w
+
+
 def down_uniforms(width=8, height=8):
     u = vrt.default_uniforms()
     u.camPos[:] = [7.3, 10.6, 7.7]
@@ -124,6 +135,14 @@ def test_overbright_clamp_position_follows_the_shader_loop(oracle):
     assert (shade > np.float32(1.25)).all() and (cast == 1 | (2 << 15)).all()  # no test after light 15
     shade, cast = run((), diffuse=2.0)
     assert (shade == np.float32(1.25)).all() and (cast == 1).all()
+
+
+def test_palette_scene_shows_every_voxel(oracle):
+    u = down_uniforms(48, 48)
+    u.camPos[:] = [8.0, 12.5, 8.0]
+    u.rotateMatrix[:] = vrt.rotate_matrix(1.5707, 0.0)
+    out = oracle.render(palette_floor_world(), S, S, u, 48, 48)
+    assert len(set(out["hit"][out["hit"] >= 0].tolist())) == 256
 
 
 def test_inactive_and_far_lights_are_not_cast(oracle):
@@ -205,6 +224,11 @@ def kat_scenes():
     u.rotateMatrix[:] = vrt.rotate_matrix(-math.atan(1.0), math.radians(45.0))
     u.maxSteps = 40
     scenes.append(("ties", world([(0, 0, 5), (6, 6, 6), (4, 4, 9)]), u, 9, 9))
+    # every channel value 0..255 on screen, seen from straight above
+    u = down_uniforms(48, 48)
+    u.camPos[:] = [8.0, 12.5, 8.0]
+    u.rotateMatrix[:] = vrt.rotate_matrix(1.5707, 0.0)
+    scenes.append(("palette", palette_floor_world(), u, 48, 48))
     # capped and zero-step rays
     u = down_uniforms(4, 4)
     u.maxSteps = 0

@@ -767,6 +767,29 @@ __device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
     return lo;
 }
 
+// fl(i / 255) for i = 0..255: the shader's channel scale (fshader.glsl:184-186), filled on
+// each device by init_div255_kernel with the same IEEE division, so a table read gives
+// the quotient bit for bit.
+__device__ float g_div255[256];
+
+__global__ void init_div255_kernel() { g_div255[threadIdx.x] = fdiv((float)threadIdx.x, 255.0f); }
+
+// pack_color of the tile kernel: the channel quotients come from g_div255.
+__device__ __forceinline__ uint32_t pack_color_tab(const vrt_uniforms& u, bool hit, int32_t word, float mr,
+                                                   float mg, float mb, int primary_steps) {
+    float c0, c1, c2;
+    if (u.viewDepthField == 1) {
+        c0 = c1 = c2 = fdiv((float)primary_steps, 100.0f);
+    } else if (hit) {
+        c0 = fmul(__ldg(g_div255 + ((word & 0x00FF0000) >> 16)), mr);
+        c1 = fmul(__ldg(g_div255 + ((word & 0x0000FF00) >> 8)), mg);
+        c2 = fmul(__ldg(g_div255 + (word & 0x000000FF)), mb);
+    } else {
+        c0 = 0.6f; c1 = 0.7f; c2 = 0.8f;
+    }
+    return to_u8(c0) | (to_u8(c1) << 8) | (to_u8(c2) << 16) | (to_u8(1.0f) << 24);
+}
+
 // The local lights that may be in range of some lane of the warp, as a warp-uniform bit
 // mask: lane l < 16 tests light l's cube of half-size R1 + 1 against the integer
 // bounding box of the warp's hit points (every lane must call this).  A light a lane
@@ -796,8 +819,9 @@ __device__ __forceinline__ unsigned warp_light_candidates(const vrt_uniforms& u,
 
 // One CTA per ray tile (tile_w x tile_h pixels, tile_w*tile_h == blockDim.x) over the tile
 // space of every view of the launch: a single frame, or a batch of cameras of any sizes.
-// EXACT launches (any view asking for step counts) step every ray to its end.
-template <bool EXACT>
+// EXACT launches (any view asking for step counts) step every ray to its end; DEBUG
+// launches (any view with a debug output) write the per-pixel side outputs.
+template <bool EXACT, bool DEBUG>
 __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_constant__ MaskParams P) {
     __shared__ int2 alive[24];
     fill_alive_ranges(alive, P, EXACT);
@@ -903,8 +927,9 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
         res.hit = pr == T_HIT ? hit : -1;
         res.steps = steps;
         res.mr = mr; res.mg = mg; res.mb = mb;
-        res.rgba = pack_color(u, pr == T_HIT, word, mr, mg, mb, res.primary_steps);
-        store_pixel(V.dbg, V.rgba, (uint64_t)py * V.width + px, res);
+        res.rgba = pack_color_tab(u, pr == T_HIT, word, mr, mg, mb, res.primary_steps);
+        if (DEBUG) store_pixel(V.dbg, V.rgba, (uint64_t)py * V.width + px, res);
+        else reinterpret_cast<uint32_t*>(V.rgba)[(uint64_t)py * V.width + px] = res.rgba;
     }
     if (V.stats) {
         unsigned rays = valid ? 1u + __popc(res.cast) : 0u;
@@ -1073,7 +1098,13 @@ static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, 
         P.cl[a] = exact ? 0 : std::max(0, std::min(P.bb[a], dims[a]));
         P.cl[3 + a] = exact ? dims[a] : std::min(dims[a], std::max(P.bb[3 + a] + 1, P.cl[a]));
     }
-    auto kern = exact ? render_tiles_kernel<true> : render_tiles_kernel<false>;
+    bool debug = false;
+    for (int i = 0; i < nviews; i++) {
+        const vrt_debug_out& d = h_views[i].dbg;
+        debug |= d.hit_index || d.cast_mask || d.occ_mask || d.steps || d.primary_steps || d.shade;
+    }
+    auto kern = exact ? (debug ? render_tiles_kernel<true, true> : render_tiles_kernel<true, false>)
+                      : (debug ? render_tiles_kernel<false, true> : render_tiles_kernel<false, false>);
     P.tile0 = tile0;
     if (ntiles < 0) ntiles = total_tiles - tile0;
     if (ntiles > 0) kern<<<ntiles, threads, 0, s>>>(P);
@@ -1115,6 +1146,19 @@ static int ensure_views(vrt_renderer* r, int n) {
 
 extern "C" {
 
+// Fill g_div255 on the current device once; every tile-kernel launch goes through a renderer.
+static int ensure_div255(int device) {
+    static std::mutex mu;
+    static bool done[64] = {};
+    std::lock_guard<std::mutex> lock(mu);
+    if (device >= 0 && device < 64 && done[device]) return VRT_OK;
+    init_div255_kernel<<<1, 256>>>();
+    VRT_CUDA(cudaGetLastError());
+    VRT_CUDA(cudaDeviceSynchronize());  // later launches may run on any stream
+    if (device >= 0 && device < 64) done[device] = true;
+    return VRT_OK;
+}
+
 int vrt_renderer_create(vrt_renderer** out) {
     if (!out) return set_error(VRT_EINVAL, "out is NULL");
     *out = nullptr;
@@ -1124,8 +1168,15 @@ int vrt_renderer_create(vrt_renderer** out) {
     if (e == cudaSuccess) e = cudaMalloc(&r->d_counter, 256);
     if (e == cudaSuccess) e = cudaMemset(r->d_counter, 0, 256);
     if (e != cudaSuccess) {
+        cudaFree(r->d_counter);
         delete r;
         return cuda_error(e, "vrt_renderer_create");
+    }
+    const int st = ensure_div255(r->device);
+    if (st) {
+        cudaFree(r->d_counter);
+        delete r;
+        return st;
     }
     *out = r;
     return VRT_OK;
