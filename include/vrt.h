@@ -262,20 +262,22 @@ typedef struct vrt_view {
                                tile_w*tile_h must equal the launch's tile size */
 } vrt_view;
 
-/* Many cameras (uneven sizes, possibly different worlds without depth fields) in one
- * persistent launch of the occupancy-mask kernel; tiles are handed out dynamically. */
+/* Many cameras of one world without depth-field words, of uneven sizes, in one launch:
+ * the tile kernel over every view's ray tiles (each view may pick its own tile shape of
+ * the launch's thread count), or with VRT_KERNEL_BITMASK the persistent kernel, which
+ * hands tiles out from a counter. */
 int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count,
                      const vrt_render_opts* opts, void* stream);
 
 /* vrt_render_batch for callers that may not allocate device memory -- for example a
  * plugin whose host application owns every device allocation, or a frame loop that
  * cannot afford cudaMalloc's implicit device synchronisation.  It has no counterpart in
- * the reference.  It takes no renderer: its scratch (the tile counter and the view table)
- * lives in a static device array of the library, about 46 KiB per GPU, so it calls no
- * cudaMalloc or cudaFree.  At most VRT_NOALLOC_MAX_VIEWS views per call (more:
- * VRT_ERANGE).  The first call on each device looks up the array's device address
- * (cudaGetSymbolAddress) with that device current; make that first call before any stream
- * capture.  Every call shares the one array and resets its counter, so calls that overlap
+ * the reference.  It takes no renderer: its scratch (the view table, and the tile counter
+ * of the persistent kernel) lives in a static device array of the library, about 46 KiB
+ * per GPU, so it calls no cudaMalloc or cudaFree.  At most VRT_NOALLOC_MAX_VIEWS views per
+ * call (more: VRT_ERANGE).  The first call on each device looks up the array's device
+ * address (cudaGetSymbolAddress) and fills a 1 KiB table of the library, with that device
+ * current; make that first call before any stream capture.  Every call shares the one array and resets its counter, so calls that overlap
  * on the GPU (other streams, other threads) race: order them on one stream. */
 #define VRT_NOALLOC_MAX_VIEWS 64
 int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, const vrt_render_opts* opts, void* stream);

@@ -1547,7 +1547,10 @@ extern "C" int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, co
     const vrt_world* w = views[0].world;
     if (!w) return set_error(VRT_EINVAL, "view 0 has no world");
     if (w->has_depth_field) return set_error(VRT_ESTATE, "batched rendering needs a world without depth-field words");
-    const Tuning t = tuning_of(opts);
+    Tuning t;
+    bool tile_kernel = true;  // as vrt_render_batch: the tile kernel unless the persistent one is asked for
+    int st = batch_tuning(opts, &t, &tile_kernel);
+    if (st) return st;
     ViewDev hv[kNoAllocMaxViews];  // host copy of the view table, on the stack
     int tiles = 0;
     for (int i = 0; i < count; i++) {
@@ -1555,20 +1558,33 @@ extern "C" int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, co
         if (v.world != w) return set_error(VRT_EINVAL, "view %d renders another world; one batch = one world", i);
         if (!v.d_rgba || v.width < 1 || v.height < 1 || v.width > 32768 || v.height > 32768)
             return set_error(VRT_EINVAL, "view %d: bad image", i);
-        int st = check_uniforms(&v.uniforms);
+        st = check_uniforms(&v.uniforms);
         if (st) return st;
-        fill_view(hv[i], v.uniforms, v.width, v.height, v.d_rgba, nullptr, v.d_stats, t, tiles);
-        tiles += tiles_of(v.width, v.height, t);
+        Tuning tv = t;
+        if (tile_kernel && (v.tile_w > 0 || v.tile_h > 0)) {
+            if (v.tile_w < 1 || v.tile_h < 1 || v.tile_w * v.tile_h != t.tile_w * t.tile_h)
+                return set_error(VRT_EINVAL, "view %d: tile %dx%d does not have the launch's %d threads", i, v.tile_w,
+                                 v.tile_h, t.tile_w * t.tile_h);
+            tv.tile_w = v.tile_w;
+            tv.tile_h = v.tile_h;
+        }
+        fill_view(hv[i], v.uniforms, v.width, v.height, v.d_rgba, nullptr, v.d_stats, tv, tiles);
+        tiles += tiles_of(v.width, v.height, tv);
     }
     void* scratch = nullptr;
-    int st = noalloc_scratch(&scratch);
+    st = noalloc_scratch(&scratch);
     if (st) return st;
     unsigned int* d_counter = reinterpret_cast<unsigned int*>(scratch);
     ViewDev* d_views = reinterpret_cast<ViewDev*>(static_cast<unsigned char*>(scratch) + kNoAllocCounterBytes);
     if (count > 1)  // pageable source: the copy is staged before the call returns
         VRT_CUDA(cudaMemcpyAsync(d_views, hv, sizeof(ViewDev) * count, cudaMemcpyHostToDevice, S(stream)));
-    vrt_renderer shape;  // only its SM count is read by the launch
+    vrt_renderer shape;  // only its device and SM count are read
     VRT_CUDA(cudaGetDevice(&shape.device));
+    if (tile_kernel) {
+        st = ensure_div255(shape.device);  // once per device, like the scratch address
+        if (st) return st;
+        return launch_tiles(w, hv, count, tiles, d_views, t.tile_w * t.tile_h, S(stream));
+    }
     VRT_CUDA(cudaDeviceGetAttribute(&shape.num_sms, cudaDevAttrMultiProcessorCount, shape.device));
     return launch_mask(&shape, w, hv, count, tiles, t, d_views, d_counter, S(stream));  // zeroes the counter
 }
