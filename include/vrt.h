@@ -67,7 +67,7 @@ typedef struct vrt_uniforms {
     /* ---- extensions; the defaults reproduce the reference exactly ---- */
     float localLightColor[VRT_MAX_LOCAL_LIGHTS][3]; /* per-channel factor on w; 1,1,1 = reference */
     float tanHalfFov;          /* tan(vertical fov / 2); 1.0 = the reference's 90 degrees */
-    int32_t maxSteps;          /* RENDER_DIST (384): DDA iteration cap of every ray   */
+    int32_t maxSteps;          /* RENDER_DIST (384): DDA iteration cap of every ray, at most 2^24 */
     float localLightDist;      /* LOCAL_LIGHT_DIST (64): local light radius         */
     float ambient;             /* AMBIENT (0.4)                                     */
     float diffuse;             /* DIFFUSE (0.8)                                     */

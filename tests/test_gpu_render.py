@@ -237,6 +237,11 @@ def test_bad_arguments_fail_loudly(cuda, small):
     u.maxSteps = -1
     with pytest.raises(vrt.VrtError):
         gpu_render(w, u, 8, 8)
+    u.maxSteps = (1 << 24) + 1  # beyond what the shader's float distance counter can reach
+    for k in (vrt.KERNEL_WORD, vrt.KERNEL_MASK_PIXEL):
+        with pytest.raises(vrt.VrtError) as e:
+            gpu_render(w, u, 8, 8, kernel=k)
+        assert e.value.status == vrt.EINVAL
 
 
 @pytest.mark.parametrize("radius, intensity, limit", [(6.0, 1.0, 1.25), (16.0, 3.0, 1.3), (3.0, 2.0, 1.25)])

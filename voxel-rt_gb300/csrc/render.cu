@@ -998,9 +998,15 @@ struct vrt_batch_graph {
 
 static inline cudaStream_t S(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
+// The shader counts the distance a ray travelled in a float (fshader.glsl:82-85), which
+// stops growing at 2^24: a ray stuck on a zero direction component would never reach a
+// larger cap, so caps above 2^24 are refused.
+constexpr int kMaxSteps = 1 << 24;
+
 static int check_uniforms(const vrt_uniforms* u) {
     if (!u) return set_error(VRT_EINVAL, "NULL uniforms");
-    if (u->maxSteps < 0) return set_error(VRT_EINVAL, "maxSteps %d < 0", u->maxSteps);
+    if (u->maxSteps < 0 || u->maxSteps > kMaxSteps)
+        return set_error(VRT_EINVAL, "maxSteps %d outside [0, 2^24]", u->maxSteps);
     return VRT_OK;
 }
 
