@@ -99,10 +99,11 @@ typedef struct vrt_debug_out {
 
 /* Render kernel choice. AUTO picks the per-pixel occupancy-mask kernel unless the world
  * holds depth-field words, which only the word kernel follows. */
-#define VRT_KERNEL_AUTO 0
-#define VRT_KERNEL_WORD 1     /* one thread per pixel, one 4-byte word per DDA step */
-#define VRT_KERNEL_BITMASK 2  /* occupancy-mask traversal, persistent ray refill    */
-#define VRT_KERNEL_MASK_PIXEL 3 /* occupancy-mask traversal, one thread per pixel     */
+#define VRT_KERNEL_AUTO 0       /* the tile kernel; the word kernel for worlds with depth-field words */
+#define VRT_KERNEL_WORD 1       /* one thread per pixel, one 4-byte word per DDA step     */
+#define VRT_KERNEL_BITMASK 2    /* occupancy-mask traversal, persistent ray refill (no depth-field words) */
+#define VRT_KERNEL_MASK_PIXEL 3 /* the tile kernel: occupancy-mask traversal, one thread per pixel,
+                                   following depth-field jumps too */
 
 /* Step accounting.  The occupancy-mask kernels end a ray as soon as its path provably
  * holds no solid voxel: its cell lies beyond the bounding box of the world's solid voxels
@@ -262,10 +263,10 @@ typedef struct vrt_view {
                                tile_w*tile_h must equal the launch's tile size */
 } vrt_view;
 
-/* Many cameras of one world without depth-field words, of uneven sizes, in one launch:
- * the tile kernel over every view's ray tiles (each view may pick its own tile shape of
- * the launch's thread count), or with VRT_KERNEL_BITMASK the persistent kernel, which
- * hands tiles out from a counter. */
+/* Many cameras of one world, of uneven sizes, in one launch: the tile kernel over every
+ * view's ray tiles (each view may pick its own tile shape of the launch's thread count),
+ * or with VRT_KERNEL_BITMASK the persistent kernel, which hands tiles out from a counter
+ * and needs a world without depth-field words. */
 int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count,
                      const vrt_render_opts* opts, void* stream);
 
@@ -282,8 +283,9 @@ int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count,
 #define VRT_NOALLOC_MAX_VIEWS 64
 int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, const vrt_render_opts* opts, void* stream);
 
-/* A captured CUDA graph of vrt_render_batch over a fixed view list; replay with
- * vrt_batch_graph_launch.  Uniform or image-pointer changes need a new graph. */
+/* A captured CUDA graph of vrt_render_batch over a fixed view list of a world without
+ * depth-field words; replay with vrt_batch_graph_launch.  Uniform or image-pointer changes
+ * need a new graph; edits of the world's words do not. */
 typedef struct vrt_batch_graph vrt_batch_graph;
 int vrt_batch_graph_create(vrt_renderer* r, const vrt_view* views, int32_t count,
                            const vrt_render_opts* opts, void* stream, vrt_batch_graph** out);

@@ -1,0 +1,105 @@
+"""The tile kernel on worlds with depth-field words -- the reference's own worlds, where
+fixDepthField leaves a jump distance in almost every air voxel near a solid.  The
+kernel follows the shader's jumps (fshader.glsl:114-121) and its float distance cap
+(:83); its frames must equal the oracle's and the reference shader's golden outputs."""
+import json
+
+import numpy as np
+import pytest
+
+import vrt
+from helpers import assert_same_frame, fcolor_from_outputs, gpu_render, load_golden, make_world, uniforms_from_dict
+from test_gpu_fuzz import random_case
+
+pytestmark = pytest.mark.gpu
+
+
+def test_reference_scene(cuda, oracle):
+    case = load_golden("shader_reference_scene.npz")
+    w = vrt.World(512, 96)
+    w.init_reference()
+    w.fix_depth_field()
+    assert w.info().has_depth_field == 1
+    words = w.download(np.empty(512 * 96 * 512, np.int32))
+    u = uniforms_from_dict(json.loads(str(case["uniforms"])))
+    g = gpu_render(w, u, 800, 600, kernel=vrt.KERNEL_MASK_PIXEL)
+    px, py = case["px"], case["py"]
+    assert np.array_equal(g["hit"][py, px], case["hit"])
+    assert np.array_equal(g["steps"][py, px], case["steps"])
+    col = fcolor_from_outputs(words, g["hit"][py, px], g["shade"][py, px])
+    assert (col.view(np.uint32) == case["color_bits"][:, :3]).all()
+    o = oracle.render(words, 512, 96, u, 800, 600)
+    assert_same_frame(o, g)
+    f = gpu_render(w, u, 800, 600, kernel=vrt.KERNEL_MASK_PIXEL, debug=False)  # inexact launch
+    assert np.array_equal(f["rgba"], o["rgba"])
+    assert int(f["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"]
+
+
+def test_edits_refresh_the_stop_masks(cuda, oracle, vrt_lib):
+    W, H = 96, 48
+    w = make_world(vrt_lib.terrain_generate(W, H, 17, 2), W, H)
+    w.fix_depth_field()
+    u = vrt.default_uniforms()
+    u.camPos[:] = [20.5, 40.25, 18.5]
+    u.rotateMatrix[:] = vrt.rotate_matrix(0.6, 0.9)
+    u.lightPos[:] = [48.0, 400.0, 20.0]
+    u.maxSteps = 200
+    u.localLightDist = 24.0
+    u.localLights[0][:] = [40.5, 30.5, 44.5, 0.7]
+    u.aspectRatio = 80 / 60
+    for edit in range(3):
+        words = w.download(np.empty(W * H * W, np.int32))
+        o = oracle.render(words, W, H, u, 80, 60)
+        assert (o["hit"] >= 0).sum() > 100
+        assert_same_frame(o, gpu_render(w, u, 80, 60, kernel=vrt.KERNEL_MASK_PIXEL))
+        w.remove_sphere(40 + 9 * edit, 20, 40 - 7 * edit, 6, 1)  # with the depth-field refresh
+
+
+@pytest.mark.parametrize("seed", range(10))
+def test_random_depth_field_scenes(cuda, oracle, seed):
+    words, W, H, u, width, height = random_case(seed)
+    w = make_world(words, W, H)
+    w.fix_depth_field()
+    words = w.download(np.empty_like(words))
+    o = oracle.render(words, W, H, u, width, height)
+    for k in (vrt.KERNEL_MASK_PIXEL, vrt.KERNEL_WORD):
+        try:
+            assert_same_frame(o, gpu_render(w, u, width, height, kernel=k))
+        except AssertionError as e:
+            raise AssertionError(f"seed {seed}, kernel {k}: {e}") from None
+    g = gpu_render(w, u, width, height, kernel=vrt.KERNEL_MASK_PIXEL, debug=False)
+    assert np.array_equal(o["rgba"], g["rgba"]), f"seed {seed}: inexact launch"
+
+
+def test_batch_on_a_depth_field_world(cuda, oracle):
+    """vrt_render_batch renders a reference-format world with the tile kernel; the graph
+    and allocation-free forms refuse it (a replay would keep stale stop masks after an
+    edit, and the stop masks are allocated on first use)."""
+    import ctypes as C
+    import torch
+    W, H = 64, 32
+    w = make_world(vrt.terrain_generate(W, H, 5, 2), W, H)
+    w.fix_depth_field()
+    words = w.download(np.empty(W * H * W, np.int32))
+    cams = []
+    for i, (wd, ht) in enumerate([(40, 30), (23, 17), (64, 48)]):
+        u = vrt.default_uniforms()
+        u.camPos[:] = [10.5 + 7 * i, 28.25, 12.5 + 5 * i]
+        u.rotateMatrix[:] = vrt.rotate_matrix(0.5 + 0.1 * i, 0.7 * i)
+        u.lightPos[:] = [32.0, 300.0, 10.0]
+        u.maxSteps = 150
+        u.aspectRatio = wd / ht
+        cams.append((u, wd, ht))
+    imgs = [torch.zeros(wd * ht * 4, dtype=torch.uint8, device="cuda") for (_, wd, ht) in cams]
+    views = [vrt.make_view(w, u, wd, ht, img.data_ptr()) for (u, wd, ht), img in zip(cams, imgs)]
+    r = vrt.Renderer()
+    r.render_batch(views)
+    torch.cuda.synchronize()
+    for (u, wd, ht), img in zip(cams, imgs):
+        o = oracle.render(words, W, H, u, wd, ht)
+        assert np.array_equal(img.cpu().numpy().reshape(ht, wd, 4), o["rgba"])
+    arr = (vrt.View * len(views))(*views)
+    g = C.c_void_p()
+    stream = torch.cuda.current_stream().cuda_stream
+    assert vrt.lib().vrt_batch_graph_create(r.handle, arr, len(views), None, stream, C.byref(g)) == vrt.ESTATE
+    assert vrt.lib().vrt_render_batch_noalloc(arr, len(views), None, stream) == vrt.ESTATE

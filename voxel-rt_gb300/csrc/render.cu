@@ -683,9 +683,18 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
 // shader's comparison and its one intersect add, in the shader's order; memory is read
 // only when the ray leaves its known box.  On a hit, cd / axis / sgn / cell describe the
 // last step (currDist, hitNormal, the voxel).
+// DF (worlds with depth-field words): the masks mark every cell the shader's loop stops
+// at (word != -1).  At such a cell the word decides: solid is a hit; a depth-field word is
+// the shader's jump (:114-121): distTravelled and currDist grow by the jump, the start
+// moves to dir * currDist + start, and the walk restarts from its cell.  The step cap is
+// then the shader's float test distTravelled < min(dist, RENDER_DIST) (:83), kept as a
+// float because the jumps make distTravelled fractional.  start_out receives the start
+// the hit position is measured from.
+template <bool DF>
 __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, V3 o, V3 d, int n, int maxSteps,
                                         float& cd, int& axis, int& sgn, int& steps, int32_t& hit_index,
-                                        unsigned& refills) {
+                                        unsigned& refills, V3& start_out) {
+    start_out = o;
     RaySetup s;
     ray_setup(o, d, s);
     BoxRay r;
@@ -701,7 +710,15 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
     // this loop.  (Doing the same for the box counters helped long empty boxes but cost
     // more on the 1080p frame, so those stay plain adds.)
     const int one = P.one, four = P.four, sixteen = P.sixteen;
-    r.left = n0 - 1;  // after the top-of-loop decrement: negative on the last allowed iteration
+    // after the top-of-loop decrement r.left is negative on the last allowed iteration; with
+    // DF the float test decides instead, and r.left only counts (it cannot reach 0 first:
+    // caps are at most 2^24)
+    constexpr int kCount = 1 << 30;
+    const int left0 = DF ? kCount - 1 : n0 - 1;
+    r.left = left0;
+    float travelled = 0.0f;
+    const float lim = DF ? fminf((float)n, (float)maxSteps) : 0.0f;
+    V3 start = o;
     // no box yet: the first step along any axis (even one with s == 0) triggers a lookup
     r.kx = 0; r.ky = 0; r.kz = 0;
     r.ex = s.cx + s.sx; r.ey = s.cy + s.sy; r.ez = s.cz + s.sz;
@@ -716,6 +733,11 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
         if (by) r.ky -= 1;
         if (bz) r.kz -= 1;
         r.left -= 1;
+        bool last = false;  // DF: no iteration follows this one
+        if (DF) {
+            travelled = fadd(travelled, 1.0f);
+            last = !(travelled < lim);
+        }
         bool hb = false;  // the cell's bit, meaningful only while the step stays in the box
         if (r.m) {
             if (bx) r.bi = r.bi * one + r.sx;
@@ -723,7 +745,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
             if (bz) r.bi = r.sz * sixteen + r.bi;
             hb = (r.m >> (r.bi & 63)) & 1;
         }
-        if (((r.kx | r.ky | r.kz | r.left) < 0) | hb) {
+        if (((r.kx | r.ky | r.kz | r.left) < 0) | hb | last) {
             const int a = bx ? 0 : (by ? 1 : 2);
             const bool out = (r.kx | r.ky | r.kz) < 0;
             if (out) {
@@ -740,19 +762,44 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
             } else {
                 result = T_MISS;  // the step cap: this was the last iteration
             }
+            if (DF && result == T_HIT) {
+                const int32_t v = __ldg(P.words + hit_index);
+                if (v < 0) {  // a depth-field word: jump (fshader.glsl:114-121)
+                    const float toJump = -__int_as_float(v);
+                    travelled = fadd(travelled, toJump);
+                    const float cdj = fadd(a == 0 ? r.tx : (a == 1 ? r.ty : r.tz), toJump);
+                    start = add3(mul3s(d, cdj), start);
+                    const int ncx = f2i(start.x), ncy = f2i(start.y), ncz = f2i(start.z);
+                    r.tx = fdiv(fsub((float)(ncx + (r.sx > 0)), start.x), d.x);
+                    r.ty = fdiv(fsub((float)(ncy + (r.sy > 0)), start.y), d.y);
+                    r.tz = fdiv(fsub((float)(ncz + (r.sz > 0)), start.z), d.z);
+                    // no box yet: the first step from the new cell looks one up
+                    r.kx = 0; r.ky = 0; r.kz = 0;
+                    r.ex = ncx + r.sx; r.ey = ncy + r.sy; r.ez = ncz + r.sz;
+                    r.m = 0;
+                    r.bi = 0;
+                    hit_index = -1;
+                    if (!(travelled < lim)) {
+                        result = T_MISS;
+                        break;
+                    }
+                    continue;  // the jump replaced this iteration's intersect add
+                }
+            }
             if (result != T_LIVE) {
                 axis = a;
                 cd = a == 0 ? r.tx : (a == 1 ? r.ty : r.tz);
                 sgn = a == 0 ? r.sx : (a == 1 ? r.sy : r.sz);
                 break;
             }
-            if (r.left < 0) { result = T_MISS; break; }  // entered a box on the last iteration
+            if (DF ? last : r.left < 0) { result = T_MISS; break; }  // entered a box on the last iteration
         }
         if (bx) r.tx = fadd(r.tx, r.dx);
         if (by) r.ty = fadd(r.ty, r.dy);
         if (bz) r.tz = fadd(r.tz, r.dz);
     }
-    steps += n0 - 1 - r.left;  // r.left = n0 - 2 - (index of the breaking iteration)
+    steps += left0 - r.left;  // r.left = left0 - 1 - (index of the breaking iteration)
+    start_out = start;
     return result;
 }
 
@@ -820,8 +867,9 @@ __device__ __forceinline__ unsigned warp_light_candidates(const vrt_uniforms& u,
 // One CTA per ray tile (tile_w x tile_h pixels, tile_w*tile_h == blockDim.x) over the tile
 // space of every view of the launch: a single frame, or a batch of cameras of any sizes.
 // EXACT launches (any view asking for step counts) step every ray to its end; DEBUG
-// launches (any view with a debug output) write the per-pixel side outputs.
-template <bool EXACT, bool DEBUG>
+// launches (any view with a debug output) write the per-pixel side outputs; DF launches
+// render a world with depth-field words (the masks are its stop masks).
+template <bool EXACT, bool DEBUG, bool DF>
 __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_constant__ MaskParams P) {
     __shared__ int2 alive[24];
     fill_alive_ranges(alive, P, EXACT);
@@ -841,13 +889,14 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
     int axis = 2, sgn = 0, steps = 0, a2 = 0, s2 = 0;
     int32_t hit = -1, dummy = -1;
     int pr = T_MISS;
+    V3 from = cam, from2;  // the start a hit position is measured from (moved by depth-field jumps)
     if (valid) {
         rd = primary_dir(u, px, py, V.width, V.height);
-        pr = cast_box(P, alive, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit, refills);
+        pr = cast_box<DF>(P, alive, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit, refills, from);
         res.primary_steps = steps;
     }
     const bool lit = valid && pr == T_HIT && u.viewDepthField != 1;
-    const V3 hp = lit ? add3(mul3s(rd, cd), cam) : V3{0.f, 0.f, 0.f};
+    const V3 hp = lit ? add3(mul3s(rd, cd), from) : V3{0.f, 0.f, 0.f};
     const unsigned cand = warp_light_candidates(u, lit, hp);
     if (valid) {
         float mr = u.ambient, mg = u.ambient, mb = u.ambient;
@@ -896,8 +945,8 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
                     }
                 }
                 if (cast) {
-                    const int sr = cast_box(P, alive, add3(hp, mul3s(dir, 0.001f)), dir, n, u.maxSteps, c2, a2, s2,
-                                            steps, dummy, refills);
+                    const int sr = cast_box<DF>(P, alive, add3(hp, mul3s(dir, 0.001f)), dir, n, u.maxSteps, c2, a2,
+                                                s2, steps, dummy, refills, from2);
                     const unsigned bit = 1u << (j + 1);
                     res.cast |= bit;
                     if (sr == T_HIT) {
@@ -1109,8 +1158,21 @@ static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, 
         const vrt_debug_out& d = h_views[i].dbg;
         debug |= d.hit_index || d.cast_mask || d.occ_mask || d.steps || d.primary_steps || d.shade;
     }
-    auto kern = exact ? (debug ? render_tiles_kernel<true, true> : render_tiles_kernel<true, false>)
-                      : (debug ? render_tiles_kernel<false, true> : render_tiles_kernel<false, false>);
+    const bool df = w->has_depth_field != 0;
+    if (df) {
+        // the stop masks are a cache of the words, rebuilt here after any change
+        const int st = refresh_stop(const_cast<vrt_world*>(w), s);
+        if (st) return st;
+        P.bricks = w->d_stop;
+        P.bdir = w->d_sdir;
+    }
+    using Kern = void (*)(MaskParams);
+    static const Kern kernels[2][2][2] = {
+        {{render_tiles_kernel<false, false, false>, render_tiles_kernel<false, false, true>},
+         {render_tiles_kernel<false, true, false>, render_tiles_kernel<false, true, true>}},
+        {{render_tiles_kernel<true, false, false>, render_tiles_kernel<true, false, true>},
+         {render_tiles_kernel<true, true, false>, render_tiles_kernel<true, true, true>}}};
+    const Kern kern = kernels[exact][debug][df];
     P.tile0 = tile0;
     if (ntiles < 0) ntiles = total_tiles - tile0;
     if (ntiles > 0) kern<<<ntiles, threads, 0, s>>>(P);
@@ -1230,9 +1292,7 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
         VRT_CUDA(cudaGetLastError());
         return VRT_OK;
     }
-    if (kernel == VRT_KERNEL_MASK_PIXEL) {
-        if (w->has_depth_field)
-            return set_error(VRT_ESTATE, "the world holds depth-field words, which only the word kernel follows");
+    if (kernel == VRT_KERNEL_MASK_PIXEL) {  // follows depth-field jumps too
         Tuning t;
         int st = tile_tuning(opts, &t);
         if (st) return st;
@@ -1297,7 +1357,7 @@ int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* 
     if (kernel == VRT_KERNEL_AUTO && !w->has_depth_field) kernel = VRT_KERNEL_MASK_PIXEL;
     int bands = 1;
     Tuning t{};
-    if (kernel == VRT_KERNEL_MASK_PIXEL && !w->has_depth_field) {
+    if (kernel == VRT_KERNEL_MASK_PIXEL) {
         st = tile_tuning(opts, &t);
         if (st) return st;
         const int tiles_y = (height + t.tile_h - 1) / t.tile_h;
@@ -1346,12 +1406,16 @@ int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* 
     return VRT_OK;
 }
 
+// allow_df: the launch follows depth-field jumps (the tile kernel, launched now rather
+// than replayed from a graph that would keep stale stop masks after an edit).
 static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, std::vector<ViewDev>& hv,
-                       const vrt_world** world_out, int* total_out) {
+                       const vrt_world** world_out, int* total_out, bool allow_df) {
     if (!views || count < 1) return set_error(VRT_EINVAL, "empty batch");
     const vrt_world* w = views[0].world;
     if (!w) return set_error(VRT_EINVAL, "view 0 has no world");
-    if (w->has_depth_field) return set_error(VRT_ESTATE, "batched rendering needs a world without depth-field words");
+    if (w->has_depth_field && !allow_df)
+        return set_error(VRT_ESTATE, "the world holds depth-field words: render it with vrt_render or vrt_render_batch "
+                                     "and the tile kernel");
     hv.resize(count);
     int tiles = 0;
     for (int i = 0; i < count; i++) {
@@ -1407,7 +1471,7 @@ int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count, cons
     std::vector<ViewDev> hv;
     const vrt_world* w = nullptr;
     int total = 0;
-    st = build_batch(views, count, t, hv, &w, &total);
+    st = build_batch(views, count, t, hv, &w, &total, tiles);
     if (st) return st;
     if (count > 1) {
         st = ensure_views(r, count);
@@ -1429,7 +1493,7 @@ int vrt_batch_graph_create(vrt_renderer* r, const vrt_view* views, int32_t count
     std::vector<ViewDev> hv;
     const vrt_world* w = nullptr;
     int total = 0;
-    st = build_batch(views, count, t, hv, &w, &total);
+    st = build_batch(views, count, t, hv, &w, &total, false);
     if (st) return st;
     vrt_batch_graph* g = new vrt_batch_graph();
     cudaError_t e = cudaMalloc(&g->d_views, sizeof(ViewDev) * (size_t)count);

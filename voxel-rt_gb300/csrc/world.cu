@@ -188,7 +188,32 @@ __global__ void dir_pass_kernel(const uint64_t* __restrict__ occ, const uint64_t
     out[self] = (res[0] & plus) | (res[1] & ~plus);
 }
 
-static int dir_passes(vrt_world* w, int bx0, int by0, int bz0, int bx1, int by1, int bz1, cudaStream_t s) {
+// One thread per brick of the whole grid: bit x+4y+16z set when the voxel's word is not
+// -1, i.e. the cells where the shader's loop stops to hit (word >= 0) or to jump (a
+// depth-field word, fshader.glsl:114-121).  Voxels outside the world are clear.
+__global__ void stop_mask_kernel(const int32_t* __restrict__ words, uint64_t* __restrict__ stop, Layout L) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= L.n_bricks) return;
+    const int bx = (int)(t % L.BWp), by = (int)((t / L.BWp) % L.BHp), bz = (int)(t / ((uint64_t)L.BWp * L.BHp));
+    uint64_t m = 0;
+    for (int dz = 0; dz < 4; dz++) {
+        const int z = bz * 4 + dz;
+        if (z >= L.W) break;
+        for (int dy = 0; dy < 4; dy++) {
+            const int y = by * 4 + dy;
+            if (y >= L.H) break;
+            const int32_t* row = words + ((uint64_t)z * L.H + y) * L.W;
+            for (int dx = 0; dx < 4; dx++) {
+                const int x = bx * 4 + dx;
+                if (x < L.W && __ldg(row + x) != -1) m |= 1ull << (dx + 4 * dy + 16 * dz);
+            }
+        }
+    }
+    stop[t] = m;  // t is the linear brick slot bx + BWp*(by + BHp*bz)
+}
+
+static int dir_passes(vrt_world* w, const uint64_t* occ, uint8_t* dst8, int bx0, int by0, int bz0, int bx1, int by1,
+                      int bz1, cudaStream_t s) {
     const Layout& L = w->L;
     const int cap = kDistCap;
     auto clampbox = [&](int& a0, int& a1, int lim) { a0 = std::max(a0, 0); a1 = std::min(a1, lim); };
@@ -200,14 +225,14 @@ static int dir_passes(vrt_world* w, int bx0, int by0, int bz0, int bx1, int by1,
     uint64_t* ta = reinterpret_cast<uint64_t*>(w->d_tmp_a);
     uint64_t* tb = reinterpret_cast<uint64_t*>(w->d_tmp_b);
     uint64_t n = (uint64_t)(X1 - X0) * (ya1 - ya0) * (za1 - za0);
-    dir_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_bricks, nullptr, ta, L, 0, X0, ya0, za0, X1 - X0,
-                                                       ya1 - ya0, za1 - za0, 1);
+    dir_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(occ, nullptr, ta, L, 0, X0, ya0, za0, X1 - X0, ya1 - ya0,
+                                                       za1 - za0, 1);
     n = (uint64_t)(X1 - X0) * (Y1 - Y0) * (za1 - za0);
-    dir_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_bricks, ta, tb, L, 1, X0, Y0, za0, X1 - X0, Y1 - Y0,
-                                                       za1 - za0, 0);
+    dir_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(occ, ta, tb, L, 1, X0, Y0, za0, X1 - X0, Y1 - Y0, za1 - za0,
+                                                       0);
     n = (uint64_t)(X1 - X0) * (Y1 - Y0) * (Z1 - Z0);
-    dir_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_bricks, tb, reinterpret_cast<uint64_t*>(w->d_bdir), L,
-                                                       2, X0, Y0, Z0, X1 - X0, Y1 - Y0, Z1 - Z0, 0);
+    dir_pass_kernel<<<blocks_for(n, 256), 256, 0, s>>>(occ, tb, reinterpret_cast<uint64_t*>(dst8), L, 2, X0, Y0, Z0,
+                                                       X1 - X0, Y1 - Y0, Z1 - Z0, 0);
     VRT_CUDA(cudaGetLastError());
     return VRT_OK;
 }
@@ -226,9 +251,34 @@ static int region_passes(vrt_world* w, cudaStream_t s) {
 // the distances of all regions (a few thousand to a few hundred thousand bytes).
 static int refresh_distances(vrt_world* w, int bx0, int by0, int bz0, int bx1, int by1, int bz1, cudaStream_t s) {
     const int cap = kDistCap;
-    int st = dir_passes(w, bx0 - cap, by0 - cap, bz0 - cap, bx1 + cap, by1 + cap, bz1 + cap, s);
+    int st = dir_passes(w, w->d_bricks, w->d_bdir, bx0 - cap, by0 - cap, bz0 - cap, bx1 + cap, by1 + cap, bz1 + cap,
+                        s);
     if (st) return st;
     return region_passes(w, s);
+}
+
+int refresh_stop(vrt_world* w, cudaStream_t s) {
+    if (!w->stop_stale) return VRT_OK;
+    const Layout& L = w->L;
+    if (!w->d_stop) {
+        cudaError_t e = cudaMalloc(&w->d_stop, L.n_bricks * 8);
+        if (e == cudaSuccess) e = cudaMalloc(&w->d_sdir, L.n_bricks * 8);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(w->d_stop);
+            cudaFree(w->d_sdir);
+            w->d_stop = nullptr;
+            w->d_sdir = nullptr;
+            return set_error(VRT_ENOMEM, "stop masks: %s", cudaGetErrorString(e));
+        }
+        w->device_bytes += L.n_bricks * 16;
+    }
+    stop_mask_kernel<<<blocks_for(L.n_bricks, 256), 256, 0, s>>>(w->d_words, w->d_stop, L);
+    VRT_CUDA(cudaGetLastError());
+    const int st = dir_passes(w, w->d_stop, w->d_sdir, 0, 0, 0, L.BWp, L.BHp, L.BWp, s);
+    if (st) return st;
+    w->stop_stale = false;
+    return VRT_OK;
 }
 
 int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int z1, cudaStream_t s) {
@@ -236,6 +286,7 @@ int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int 
     x0 = std::max(x0, 0); y0 = std::max(y0, 0); z0 = std::max(z0, 0);
     x1 = std::min(x1, L.W); y1 = std::min(y1, L.H); z1 = std::min(z1, L.W);
     if (x0 >= x1 || y0 >= y1 || z0 >= z1) return VRT_OK;
+    w->stop_stale = true;
     int bx0 = x0 >> 2, by0 = y0 >> 2, bz0 = z0 >> 2;
     int bx1 = (x1 + 3) >> 2, by1 = (y1 + 3) >> 2, bz1 = (z1 + 3) >> 2;
     uint64_t nb = (uint64_t)(bx1 - bx0) * (by1 - by0) * (bz1 - bz0);
@@ -509,6 +560,8 @@ int vrt_world_destroy(vrt_world* w) {
     cudaFree(w->d_supers);
     cudaFree(w->d_rdist);
     cudaFree(w->d_bdir);
+    cudaFree(w->d_stop);
+    cudaFree(w->d_sdir);
     cudaFree(w->d_tmp_a);
     cudaFree(w->d_tmp_b);
     cudaFree(w->d_flag);
