@@ -180,7 +180,10 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-extras", action="store_true", help="skip the batched / served / CPU legs")
-    ap.add_argument("--kernel", default="pixel", choices=["pixel", "mask", "word"])
+    ap.add_argument("--kernel", default="pixel", choices=["pixel", "mask", "word", "auto"])
+    ap.add_argument("--workload", default="full", choices=["full", "reference"],
+                    help="full: the 1080p/16-light frame; reference: the reference's own world (initVoxels + "
+                         "fixDepthField on the device) at 800x600, 384 steps, rendered by the kernel AUTO picks")
     ap.add_argument("--tile", default="8x16")
     ap.add_argument("--refill", type=int, default=8)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
@@ -212,12 +215,21 @@ def main():
     sh = stream.cuda_stream
 
     threads = max(1, (os.cpu_count() or 1) // max(1, world_size))
-    sc = scenes.full(2, threads=threads)
-    world = vrt.World(sc.W, sc.H)
-    world.upload(sc.words)
+    if args.workload == "reference":
+        sc = reference_scene(vrt, scenes, np)
+        world = sc.world
+        args.no_extras = True  # the batched / served / stress legs use the full workload's world
+        if args.kernel == "pixel":
+            args.kernel = "auto"
+    else:
+        sc = scenes.full(2, threads=threads)
+        sc.data = "synthetic (seeded terrain, seed 2)"
+        world = vrt.World(sc.W, sc.H)
+        world.upload(sc.words)
     r = vrt.Renderer()
     opts = vrt.RenderOpts()
-    opts.kernel = {"pixel": vrt.KERNEL_MASK_PIXEL, "mask": vrt.KERNEL_BITMASK, "word": vrt.KERNEL_WORD}[args.kernel]
+    opts.kernel = {"pixel": vrt.KERNEL_MASK_PIXEL, "mask": vrt.KERNEL_BITMASK, "word": vrt.KERNEL_WORD,
+                   "auto": vrt.KERNEL_AUTO}[args.kernel]
     opts.tile_w, opts.tile_h = (int(v) for v in args.tile.split("x"))
     opts.refill_min = args.refill
     opts.blocks_per_sm = args.blocks_per_sm
@@ -279,9 +291,11 @@ def main():
     peak, peak_src = measured_peaks()
     algo_bytes = 4 * steps + 4 * hits + 4 * pixels
     achieved = algo_bytes / (ms * 1e-3) / 1e9
-    kname = {"pixel": "render_tiles_kernel", "mask": "render_mask_kernel", "word": "render_word_kernel"}[args.kernel]
+    kauto = "word" if world.info().has_depth_field else "pixel"
+    kname = {"pixel": "render_tiles_kernel", "mask": "render_mask_kernel", "word": "render_word_kernel"}[
+        kauto if args.kernel == "auto" else args.kernel]
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": load_traffic(kname, "full"), "peak_source": peak_src,
+                "traffic": load_traffic(kname, args.workload), "peak_source": peak_src,
                 "algorithmic_bytes_per_launch": algo_bytes, "kernel": kname,
                 "note": "effective bytes: one 4-byte word per DDA iteration of the shader (S counted exactly on the "
                         "device, equal to the oracle's) + the colour word per primary hit + the RGBA8 store; the mask "
@@ -291,7 +305,7 @@ def main():
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
-        "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded terrain, seed 2)",
+        "vs_baseline": None, "dtype": "f32", "data": sc.data,
         "config": {"workload": sc.workload, "rays_per_frame": rays, "dda_steps_per_frame": steps,
                    "dda_steps_performed": steps_performed, "box_lookups": int(st_fast[4]),
                    "primary_hits": hits, "pixels": pixels, "kernel": kname, "tile": args.tile,
@@ -312,12 +326,31 @@ def main():
         line["served"] = bench_served(vrt, torch, scenes, sc, world)
         line["served"]["plain_frame_ms"] = ms
         line["stress"] = bench_stress(vrt, torch, scenes, dev, stream)
+    if rank == 0 and world_size == 1 and (not args.no_extras or args.workload == "reference"):
         line["cpu_baseline"] = cpu_baseline(sc, args.cpu_seconds, os.cpu_count() or 1)
     if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.destroy_process_group()
     return 0
+
+
+def reference_scene(vrt, scenes, np):
+    """The reference app's first frame: its own world (initVoxels + fixDepthField, built
+    on the device), camera (195, 55, 155), the rotated sun, 800x600, RENDER_DIST 384."""
+    class Scene:
+        pass
+    sc = Scene()
+    sc.W, sc.H, sc.width, sc.height = 512, 96, 800, 600
+    sc.world = vrt.World(sc.W, sc.H)
+    sc.world.init_reference()
+    sc.world.fix_depth_field()
+    sc.words = sc.world.download(np.empty(sc.W * sc.H * sc.W, np.int32))
+    sc.uniforms = scenes.reference_scene_uniforms()
+    sc.uniforms.aspectRatio = sc.width / sc.height
+    sc.workload = "reference: initVoxels + fixDepthField 512x96x512, 800x600, 384 steps, no local lights"
+    sc.data = "the reference's own world (initVoxels + fixDepthField, built on the device)"
+    return sc
 
 
 def C_sizeof_uniforms():

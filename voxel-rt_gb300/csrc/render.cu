@@ -37,6 +37,56 @@ struct WordParams {
     unsigned long long* stats;
 };
 
+// fl(i / 255) for i = 0..255: the shader's channel scale (fshader.glsl:184-186), filled on
+// each device by init_div255_kernel with the same IEEE division, so a table read gives
+// the quotient bit for bit.
+__device__ float g_div255[256];
+
+__global__ void init_div255_kernel() { g_div255[threadIdx.x] = fdiv((float)threadIdx.x, 255.0f); }
+
+// pack_color of the tile kernel: the channel quotients come from g_div255.
+__device__ __forceinline__ uint32_t pack_color_tab(const vrt_uniforms& u, bool hit, int32_t word, float mr,
+                                                   float mg, float mb, int primary_steps) {
+    float c0, c1, c2;
+    if (u.viewDepthField == 1) {
+        c0 = c1 = c2 = fdiv((float)primary_steps, 100.0f);
+    } else if (hit) {
+        c0 = fmul(__ldg(g_div255 + ((word & 0x00FF0000) >> 16)), mr);
+        c1 = fmul(__ldg(g_div255 + ((word & 0x0000FF00) >> 8)), mg);
+        c2 = fmul(__ldg(g_div255 + (word & 0x000000FF)), mb);
+    } else {
+        c0 = 0.6f; c1 = 0.7f; c2 = 0.8f;
+    }
+    return to_u8(c0) | (to_u8(c1) << 8) | (to_u8(c2) << 16) | (to_u8(1.0f) << 24);
+}
+
+// The local lights that may be in range of some lane of the warp, as a warp-uniform bit
+// mask: lane l < 16 tests light l's cube of half-size R1 + 1 against the integer
+// bounding box of the warp's hit points (every lane must call this).  A light a lane
+// would accept (every |L - hitPos| component within R1, fshader.glsl:168-171 with the
+// pre-reject above) lies within that box grown by R1 + 1, so no candidate is lost; an
+// inactive light (a coordinate < 0, :167) never is one.
+__device__ __forceinline__ unsigned warp_light_candidates(const vrt_uniforms& u, bool lit, V3 hp) {
+    const unsigned full = 0xffffffffu;
+    const int x0 = __reduce_min_sync(full, lit ? (int)floorf(hp.x) : INT_MAX);
+    const int y0 = __reduce_min_sync(full, lit ? (int)floorf(hp.y) : INT_MAX);
+    const int z0 = __reduce_min_sync(full, lit ? (int)floorf(hp.z) : INT_MAX);
+    const int x1 = __reduce_max_sync(full, lit ? (int)floorf(hp.x) + 1 : INT_MIN);
+    const int y1 = __reduce_max_sync(full, lit ? (int)floorf(hp.y) + 1 : INT_MIN);
+    const int z1 = __reduce_max_sync(full, lit ? (int)floorf(hp.z) + 1 : INT_MIN);
+    const int lane = threadIdx.x & 31;
+    bool c = false;
+    if (x0 != INT_MAX && lane < VRT_MAX_LOCAL_LIGHTS) {
+        const float* L = u.localLights[lane];
+        if (L[0] >= 0 && L[1] >= 0 && L[2] >= 0) {
+            const float g = fabsf(u.localLightDist) * 1.0009765625f + 2.0f;
+            c = L[0] + g >= (float)x0 && L[0] - g <= (float)x1 && L[1] + g >= (float)y0 && L[1] - g <= (float)y1 &&
+                L[2] + g >= (float)z0 && L[2] - g <= (float)z1;
+        }
+    }
+    return __ballot_sync(full, c);
+}
+
 struct WordRay {
     int32_t hit;   // voxel index or -1
     float cd;      // currDist at the hit
@@ -87,17 +137,26 @@ __device__ WordRay cast_word(const int32_t* __restrict__ words, const Layout& L,
     return o;
 }
 
+template <bool DEBUG>
 __global__ void __launch_bounds__(128) render_word_kernel(const int32_t* __restrict__ words, Layout L,
                                                           const __grid_constant__ WordParams p) {
     const int px = blockIdx.x * 16 + (threadIdx.x & 15);
     const int py = blockIdx.y * 8 + (threadIdx.x >> 4);
     const bool valid = px < p.width && py < p.height;
     PixelResult res{};
+    const vrt_uniforms& u = p.u;
+    const V3 cam{u.camPos[0], u.camPos[1], u.camPos[2]};
+    V3 rd{0.f, 0.f, 0.f};
+    WordRay pr;
+    pr.hit = -1; pr.cd = 0.f; pr.axis = 2; pr.s = 0; pr.start = cam; pr.steps = 0;
     if (valid) {
-        const vrt_uniforms& u = p.u;
-        V3 cam{u.camPos[0], u.camPos[1], u.camPos[2]};
-        V3 rd = primary_dir(u, px, py, p.width, p.height);
-        WordRay pr = cast_word(words, L, cam, rd, u.maxSteps, u.maxSteps);
+        rd = primary_dir(u, px, py, p.width, p.height);
+        pr = cast_word(words, L, cam, rd, u.maxSteps, u.maxSteps);
+    }
+    const bool lit = valid && pr.hit >= 0 && u.viewDepthField != 1;
+    const V3 hp = lit ? add3(mul3s(rd, pr.cd), pr.start) : V3{0.f, 0.f, 0.f};
+    const unsigned cand = warp_light_candidates(u, lit, hp);
+    if (valid) {
         res.hit = pr.hit;
         res.steps = pr.steps;
         res.primary_steps = pr.steps;
@@ -106,7 +165,6 @@ __global__ void __launch_bounds__(128) render_word_kernel(const int32_t* __restr
         if (u.viewDepthField == 1) {
             mr = mg = mb = fdiv((float)pr.steps, 100.0f);
         } else if (pr.hit >= 0) {
-            V3 hp = add3(mul3s(rd, pr.cd), pr.start);
             V3 hn = axis_normal(pr.axis, pr.s);
             V3 lp{u.lightPos[0], u.lightPos[1], u.lightPos[2]};
             V3 toLight = norm3(sub3(lp, hp));
@@ -119,38 +177,52 @@ __global__ void __launch_bounds__(128) render_word_kernel(const int32_t* __restr
             } else {
                 res.occ |= 1u;
             }
+            // the warp's candidate local lights in ascending order, the overbright test before
+            // each and once more after the last if the shader's loop had iterations left
+            // (the same reasoning as in the tile kernel)
             const float ob = u.maxOverbright, R = u.localLightDist;
-            for (int i = 0; i < VRT_MAX_LOCAL_LIGHTS; i++) {
+            const float R1 = fadd(fmul(fabsf(R), 1.0009765625f), 1.0f);
+            unsigned todo = cand;
+            int last = -1;
+            bool clamped = false;
+            while (todo) {
+                const int i = __ffs(todo) - 1;
+                todo &= todo - 1;
+                last = i;
                 if (mr >= ob && mg >= ob && mb >= ob) {
                     mr = mg = mb = ob;
+                    clamped = true;
                     break;
-                } else if (u.localLights[i][0] >= 0 && u.localLights[i][1] >= 0 && u.localLights[i][2] >= 0) {
-                    V3 Lp{u.localLights[i][0], u.localLights[i][1], u.localLights[i][2]};
-                    float ld = len3(sub3(Lp, hp));
-                    if (ld <= R) {
-                        V3 tl = norm3(sub3(Lp, hp));
-                        WordRay lr = cast_word(words, L, add3(hp, mul3s(tl, 0.001f)), tl, f2i(fadd(ld, 1.0f)),
-                                               u.maxSteps);
-                        res.steps += lr.steps;
-                        res.cast |= 2u << i;
-                        if (lr.hit < 0) {
-                            float nl = fmax0(dot3(hn, tl));
-                            float fall = fdiv(fsub(R, ld), R);
-                            float a = u.localLights[i][3];
-                            mr = fadd(mr, fmul(fmul(fmul(a, u.localLightColor[i][0]), nl), fall));
-                            mg = fadd(mg, fmul(fmul(fmul(a, u.localLightColor[i][1]), nl), fall));
-                            mb = fadd(mb, fmul(fmul(fmul(a, u.localLightColor[i][2]), nl), fall));
-                        } else {
-                            res.occ |= 2u << i;
-                        }
+                }
+                V3 Lp{u.localLights[i][0], u.localLights[i][1], u.localLights[i][2]};
+                const V3 dl = sub3(Lp, hp);
+                if (fabsf(dl.x) > R1 || fabsf(dl.y) > R1 || fabsf(dl.z) > R1) continue;
+                float ld = len3(dl);
+                if (ld <= R) {
+                    V3 tl = norm3(dl);
+                    WordRay lr = cast_word(words, L, add3(hp, mul3s(tl, 0.001f)), tl, f2i(fadd(ld, 1.0f)),
+                                           u.maxSteps);
+                    res.steps += lr.steps;
+                    res.cast |= 2u << i;
+                    if (lr.hit < 0) {
+                        float nl = fmax0(dot3(hn, tl));
+                        float fall = fdiv(fsub(R, ld), R);
+                        float a = u.localLights[i][3];
+                        mr = fadd(mr, fmul(fmul(fmul(a, u.localLightColor[i][0]), nl), fall));
+                        mg = fadd(mg, fmul(fmul(fmul(a, u.localLightColor[i][1]), nl), fall));
+                        mb = fadd(mb, fmul(fmul(fmul(a, u.localLightColor[i][2]), nl), fall));
+                    } else {
+                        res.occ |= 2u << i;
                     }
                 }
             }
+            if (!clamped && last < VRT_MAX_LOCAL_LIGHTS - 1 && mr >= ob && mg >= ob && mb >= ob) mr = mg = mb = ob;
             word = __ldg(words + pr.hit);
         }
         res.mr = mr; res.mg = mg; res.mb = mb;
-        res.rgba = pack_color(u, pr.hit >= 0, word, mr, mg, mb, pr.steps);
-        store_pixel(p.dbg, p.rgba, (uint64_t)py * p.width + px, res);
+        res.rgba = pack_color_tab(u, pr.hit >= 0, word, mr, mg, mb, pr.steps);
+        if (DEBUG) store_pixel(p.dbg, p.rgba, (uint64_t)py * p.width + px, res);
+        else reinterpret_cast<uint32_t*>(p.rgba)[(uint64_t)py * p.width + px] = res.rgba;
     }
     if (p.stats) {
         unsigned rays = valid ? 1u + __popc(res.cast) : 0u;
@@ -814,56 +886,6 @@ __device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
     return lo;
 }
 
-// fl(i / 255) for i = 0..255: the shader's channel scale (fshader.glsl:184-186), filled on
-// each device by init_div255_kernel with the same IEEE division, so a table read gives
-// the quotient bit for bit.
-__device__ float g_div255[256];
-
-__global__ void init_div255_kernel() { g_div255[threadIdx.x] = fdiv((float)threadIdx.x, 255.0f); }
-
-// pack_color of the tile kernel: the channel quotients come from g_div255.
-__device__ __forceinline__ uint32_t pack_color_tab(const vrt_uniforms& u, bool hit, int32_t word, float mr,
-                                                   float mg, float mb, int primary_steps) {
-    float c0, c1, c2;
-    if (u.viewDepthField == 1) {
-        c0 = c1 = c2 = fdiv((float)primary_steps, 100.0f);
-    } else if (hit) {
-        c0 = fmul(__ldg(g_div255 + ((word & 0x00FF0000) >> 16)), mr);
-        c1 = fmul(__ldg(g_div255 + ((word & 0x0000FF00) >> 8)), mg);
-        c2 = fmul(__ldg(g_div255 + (word & 0x000000FF)), mb);
-    } else {
-        c0 = 0.6f; c1 = 0.7f; c2 = 0.8f;
-    }
-    return to_u8(c0) | (to_u8(c1) << 8) | (to_u8(c2) << 16) | (to_u8(1.0f) << 24);
-}
-
-// The local lights that may be in range of some lane of the warp, as a warp-uniform bit
-// mask: lane l < 16 tests light l's cube of half-size R1 + 1 against the integer
-// bounding box of the warp's hit points (every lane must call this).  A light a lane
-// would accept (every |L - hitPos| component within R1, fshader.glsl:168-171 with the
-// pre-reject above) lies within that box grown by R1 + 1, so no candidate is lost; an
-// inactive light (a coordinate < 0, :167) never is one.
-__device__ __forceinline__ unsigned warp_light_candidates(const vrt_uniforms& u, bool lit, V3 hp) {
-    const unsigned full = 0xffffffffu;
-    const int x0 = __reduce_min_sync(full, lit ? (int)floorf(hp.x) : INT_MAX);
-    const int y0 = __reduce_min_sync(full, lit ? (int)floorf(hp.y) : INT_MAX);
-    const int z0 = __reduce_min_sync(full, lit ? (int)floorf(hp.z) : INT_MAX);
-    const int x1 = __reduce_max_sync(full, lit ? (int)floorf(hp.x) + 1 : INT_MIN);
-    const int y1 = __reduce_max_sync(full, lit ? (int)floorf(hp.y) + 1 : INT_MIN);
-    const int z1 = __reduce_max_sync(full, lit ? (int)floorf(hp.z) + 1 : INT_MIN);
-    const int lane = threadIdx.x & 31;
-    bool c = false;
-    if (x0 != INT_MAX && lane < VRT_MAX_LOCAL_LIGHTS) {
-        const float* L = u.localLights[lane];
-        if (L[0] >= 0 && L[1] >= 0 && L[2] >= 0) {
-            const float g = fabsf(u.localLightDist) * 1.0009765625f + 2.0f;
-            c = L[0] + g >= (float)x0 && L[0] - g <= (float)x1 && L[1] + g >= (float)y0 && L[1] - g <= (float)y1 &&
-                L[2] + g >= (float)z0 && L[2] - g <= (float)z1;
-        }
-    }
-    return __ballot_sync(full, c);
-}
-
 // One CTA per ray tile (tile_w x tile_h pixels, tile_w*tile_h == blockDim.x) over the tile
 // space of every view of the launch: a single frame, or a batch of cameras of any sizes.
 // EXACT launches (any view asking for step counts) step every ray to its end; DEBUG
@@ -1288,7 +1310,10 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
         if (dbg) p.dbg = *dbg;
         p.stats = reinterpret_cast<unsigned long long*>(d_stats);
         dim3 grid((width + 15) / 16, (height + 7) / 8);
-        render_word_kernel<<<grid, 128, 0, S(stream)>>>(w->d_words, w->L, p);
+        const bool debug = dbg && (dbg->hit_index || dbg->cast_mask || dbg->occ_mask || dbg->steps ||
+                                   dbg->primary_steps || dbg->shade);
+        if (debug) render_word_kernel<true><<<grid, 128, 0, S(stream)>>>(w->d_words, w->L, p);
+        else render_word_kernel<false><<<grid, 128, 0, S(stream)>>>(w->d_words, w->L, p);
         VRT_CUDA(cudaGetLastError());
         return VRT_OK;
     }
