@@ -103,3 +103,34 @@ def test_batch_on_a_depth_field_world(cuda, oracle):
     stream = torch.cuda.current_stream().cuda_stream
     assert vrt.lib().vrt_batch_graph_create(r.handle, arr, len(views), None, stream, C.byref(g)) == vrt.ESTATE
     assert vrt.lib().vrt_render_batch_noalloc(arr, len(views), None, stream) == vrt.ESTATE
+
+
+def test_two_streams_after_an_edit(cuda, oracle, vrt_lib):
+    """The first render after an edit rebuilds the stop masks on its stream; a render of the
+    same world on another stream right after it must wait for that rebuild."""
+    import torch
+    W, H = 96, 48
+    w = make_world(vrt_lib.terrain_generate(W, H, 23, 2), W, H)
+    w.fix_depth_field()
+    u = vrt.default_uniforms()
+    u.camPos[:] = [30.5, 38.25, 20.5]
+    u.rotateMatrix[:] = vrt.rotate_matrix(0.55, 0.4)
+    u.lightPos[:] = [48.0, 400.0, 20.0]
+    u.maxSteps = 200
+    u.aspectRatio = 96 / 64
+    o_opts = vrt.RenderOpts()
+    o_opts.kernel = vrt.KERNEL_MASK_PIXEL
+    r1, r2 = vrt.Renderer(), vrt.Renderer()
+    s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
+    for edit in range(3):
+        w.remove_sphere(44 + 6 * edit, 22, 46, 7, 1)
+        torch.cuda.synchronize()
+        img1 = torch.zeros(96 * 64 * 4, dtype=torch.uint8, device="cuda")
+        img2 = torch.zeros_like(img1)
+        r1.render(w, u, 96, 64, img1.data_ptr(), None, 0, o_opts, s1.cuda_stream)
+        r2.render(w, u, 96, 64, img2.data_ptr(), None, 0, o_opts, s2.cuda_stream)
+        torch.cuda.synchronize()
+        words = w.download(np.empty(W * H * W, np.int32))
+        o = oracle.render(words, W, H, u, 96, 64)
+        assert np.array_equal(img1.cpu().numpy().reshape(64, 96, 4), o["rgba"])
+        assert np.array_equal(img2.cpu().numpy().reshape(64, 96, 4), o["rgba"])

@@ -90,6 +90,7 @@ struct vrt_world {
                                     // (word != -1: solid or depth-field), made on first use
     uint8_t* d_sdir = nullptr;      // directed brick distances over the stop masks
     bool stop_stale = true;         // the stop structures predate the last change of the words
+    cudaEvent_t stop_ready = nullptr;  // recorded after each rebuild: renders on other streams wait on it
     uint8_t* d_tmp_a = nullptr;     // scratch of the distance passes (8 * n_bricks each)
     uint8_t* d_tmp_b = nullptr;
     int* d_flag = nullptr;          // has-depth-field flag written by the mask kernels
@@ -107,6 +108,7 @@ namespace vrt {
 int refresh_masks(vrt_world* w, uint64_t first, uint64_t count, cudaStream_t s);
 // Rebuild the masks of the voxel box [x0,x1)x[y0,y1)x[z0,z1) (clipped).
 int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int z1, cudaStream_t s);
-// Bring the stop masks and their directed distances up to date (allocated on first use).
+// Bring the stop masks and their directed distances up to date (allocated on first use),
+// and make stream s wait until they are: the rebuild may have run on another stream.
 int refresh_stop(vrt_world* w, cudaStream_t s);
 }  // namespace vrt

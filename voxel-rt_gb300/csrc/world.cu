@@ -258,17 +258,23 @@ static int refresh_distances(vrt_world* w, int bx0, int by0, int bz0, int bx1, i
 }
 
 int refresh_stop(vrt_world* w, cudaStream_t s) {
-    if (!w->stop_stale) return VRT_OK;
+    if (!w->stop_stale) {
+        VRT_CUDA(cudaStreamWaitEvent(s, w->stop_ready, 0));  // the last rebuild, on whichever stream
+        return VRT_OK;
+    }
     const Layout& L = w->L;
     if (!w->d_stop) {
         cudaError_t e = cudaMalloc(&w->d_stop, L.n_bricks * 8);
         if (e == cudaSuccess) e = cudaMalloc(&w->d_sdir, L.n_bricks * 8);
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->stop_ready, cudaEventDisableTiming);
         if (e != cudaSuccess) {
             cudaGetLastError();
             cudaFree(w->d_stop);
             cudaFree(w->d_sdir);
+            if (w->stop_ready) cudaEventDestroy(w->stop_ready);
             w->d_stop = nullptr;
             w->d_sdir = nullptr;
+            w->stop_ready = nullptr;
             return set_error(VRT_ENOMEM, "stop masks: %s", cudaGetErrorString(e));
         }
         w->device_bytes += L.n_bricks * 16;
@@ -277,6 +283,7 @@ int refresh_stop(vrt_world* w, cudaStream_t s) {
     VRT_CUDA(cudaGetLastError());
     const int st = dir_passes(w, w->d_stop, w->d_sdir, 0, 0, 0, L.BWp, L.BHp, L.BWp, s);
     if (st) return st;
+    VRT_CUDA(cudaEventRecord(w->stop_ready, s));
     w->stop_stale = false;
     return VRT_OK;
 }
@@ -562,6 +569,7 @@ int vrt_world_destroy(vrt_world* w) {
     cudaFree(w->d_bdir);
     cudaFree(w->d_stop);
     cudaFree(w->d_sdir);
+    if (w->stop_ready) cudaEventDestroy(w->stop_ready);
     cudaFree(w->d_tmp_a);
     cudaFree(w->d_tmp_b);
     cudaFree(w->d_flag);
