@@ -138,3 +138,40 @@ def test_budget_refuses_oversized_requests(cuda, worlds):
         big = make_world(np.full(128 * 64 * 128, -1, np.int32), 128, 64)
         add_world(srv, big)
     vrt.lib().vrt_server_destroy(srv)
+
+
+def test_depth_field_world_served(cuda, oracle, vrt_lib):
+    """A world in the reference's own format (with depth-field words) served with edits:
+    renders before and after each edit equal the oracle on the words of that moment."""
+    W, H = 64, 32
+    w = make_world(vrt_lib.terrain_generate(W, H, 8, 2), W, H)
+    w.fix_depth_field()
+    srv = make_server(slots=2, max_batch=2)
+    wid = add_world(srv, w)
+    u = vrt.default_uniforms()
+    u.camPos[:] = [20.5, 29.25, 14.5]
+    u.rotateMatrix[:] = vrt.rotate_matrix(0.6, 0.5)
+    u.lightPos[:] = [32.0, 300.0, 10.0]
+    u.maxSteps = 120
+    u.aspectRatio = 48 / 32
+    edits = [(30, 14, 34, 5), (38, 12, 30, 4)]
+    stages = [w.download(np.empty(W * H * W, np.int32))]
+    shadow = vrt.World(W, H)  # replays the edits to know each stage's words
+    shadow.upload(stages[0])
+    for (x, y, z, r) in edits:
+        shadow.remove_sphere(x, y, z, r, 1)
+        stages.append(shadow.download(np.empty(W * H * W, np.int32)))
+    outs, tag = {}, 0
+    for stage in range(len(stages)):
+        for _ in range(2):
+            outs[tag] = (np.zeros(48 * 32 * 4, np.uint8), stage)
+            submit_render(srv, wid, u, 48, 32, outs[tag][0], tag)
+            tag += 1
+        if stage < len(edits):
+            submit_edit(srv, wid, edits[stage][:3], edits[stage][3], 1000 + stage)
+    done = collect(srv, tag + len(edits))
+    assert all(done[t].status == 0 for t in done)
+    for t, (img, stage) in outs.items():
+        o = oracle.render(stages[stage], W, H, u, 48, 32)
+        assert np.array_equal(img.reshape(32, 48, 4), o["rgba"]), f"render {t} after {stage} edits"
+    vrt.check(vrt.lib().vrt_server_destroy(srv))
