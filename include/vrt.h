@@ -97,8 +97,8 @@ typedef struct vrt_debug_out {
 #define VRT_STAT_FAST 6
 #define VRT_STAT_COUNT 8
 
-/* Render kernel choice. AUTO picks the per-pixel occupancy-mask kernel unless the world
- * holds depth-field words, which only the word kernel follows. */
+/* Render kernel choice.  AUTO picks the tile kernel, or the word kernel for a world that
+ * holds depth-field words (both follow the jumps; the word kernel is faster there). */
 #define VRT_KERNEL_AUTO 0       /* the tile kernel; the word kernel for worlds with depth-field words */
 #define VRT_KERNEL_WORD 1       /* one thread per pixel, one 4-byte word per DDA step     */
 #define VRT_KERNEL_BITMASK 2    /* occupancy-mask traversal, persistent ray refill (no depth-field words) */
@@ -228,15 +228,19 @@ int vrt_terrain_generate(int32_t* host_words, int32_t width, int32_t height, uin
 int vrt_terrain_height(int32_t width, uint64_t seed, int32_t x, int32_t z);
 
 /* ---- rendering ---- */
-/* A renderer owns the device scratch of the persistent kernels (work counters,
- * counters, host staging).  One renderer per concurrently used stream. */
+/* A renderer owns per-launch scratch: the view table of batches, the persistent kernel's
+ * tile counter, the staging image and streams of vrt_render_to_host.  Creating the first
+ * renderer on a device also fills a 1 KiB table the pixel colour reads (synchronises the
+ * device once).  One renderer per concurrently used stream. */
 int vrt_renderer_create(vrt_renderer** out);
 int vrt_renderer_destroy(vrt_renderer* r);
 
 /* One frame: glDrawArrays(GL_TRIANGLES,0,6) over the fullscreen quad (main.cpp:59) with
  * the uniforms of render.cpp:289-296.  d_rgba: width*height*4 bytes, row 0 = bottom row
  * (GL order); pixel (px,py) sees vPos = ((2px+1)/width-1, (2py+1)/height-1).  dbg,
- * d_stats and opts may be NULL. */
+ * d_stats and opts may be NULL.  The tile kernel's first render of a depth-field world
+ * after its words changed also rebuilds the world's stop masks on this stream (allocated
+ * on first use). */
 int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
                int32_t height, uint8_t* d_rgba, const vrt_debug_out* dbg, uint64_t* d_stats,
                const vrt_render_opts* opts, void* stream);
