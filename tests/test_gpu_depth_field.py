@@ -134,3 +134,31 @@ def test_two_streams_after_an_edit(cuda, oracle, vrt_lib):
         o = oracle.render(words, W, H, u, 96, 64)
         assert np.array_equal(img1.cpu().numpy().reshape(64, 96, 4), o["rgba"])
         assert np.array_equal(img2.cpu().numpy().reshape(64, 96, 4), o["rgba"])
+
+
+def test_banded_host_render_after_an_edit(cuda, oracle, vrt_lib):
+    """vrt_render_to_host with the tile kernel on a depth-field world: the bands run on
+    their own streams, the first rebuilds the stop masks and the others wait for it."""
+    import torch
+    W, H = 96, 48
+    w = make_world(vrt_lib.terrain_generate(W, H, 29, 2), W, H)
+    w.fix_depth_field()
+    u = vrt.default_uniforms()
+    u.camPos[:] = [26.5, 37.25, 22.5]
+    u.rotateMatrix[:] = vrt.rotate_matrix(0.5, 0.6)
+    u.lightPos[:] = [48.0, 400.0, 20.0]
+    u.maxSteps = 200
+    width, height = 120, 300
+    u.aspectRatio = width / height
+    o_opts = vrt.RenderOpts()
+    o_opts.kernel = vrt.KERNEL_MASK_PIXEL
+    o_opts.host_bands = 5
+    r = vrt.Renderer()
+    host = torch.zeros(width * height * 4, dtype=torch.uint8, pin_memory=True)
+    for edit in range(2):
+        w.remove_sphere(40 + 8 * edit, 24, 50, 6, 1)
+        torch.cuda.synchronize()
+        r.render_to_host(w, u, width, height, host.data_ptr(), o_opts)
+        words = w.download(np.empty(W * H * W, np.int32))
+        o = oracle.render(words, W, H, u, width, height)
+        assert np.array_equal(host.numpy().reshape(height, width, 4), o["rgba"])
