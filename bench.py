@@ -7,8 +7,9 @@ count).  L2 is flushed (a 256 MiB write) before every timed frame; each frame is
 with CUDA events on the launching stream.
 
   value      Mrays/s of vrt_render (device buffers), whole job over N GPUs (replicas)
-  e2e        the same through vrt_render_to_host: uniforms in, RGBA8 image copied to
-             pinned host memory every step, wall clock
+  e2e        the same through vrt_render_to_host: uniforms in, RGBA8 image out to
+             pinned host memory every step (the kernel stores the pixels into it over the
+             host link), wall clock
   roofline   effective bytes B = 4*steps + 4*primary hits + 4*pixels per frame (one
              4-byte voxel word per DDA step in the reference shader) / kernel time,
              against the measured HBM copy bandwidth; l2 fields against a measured L2
@@ -286,7 +287,9 @@ def main():
         r.render_to_host(world, sc.uniforms, W, H, host.data_ptr(), opts, sh)
     e2e_s = replicas.max_over_ranks((time.perf_counter() - t0) / args.steps, dist, dev)
     e2e = {"value": replicas.whole_job_rate(rays, e2e_s, world_size) / 1e6, "unit": UNIT, "ms_per_step": e2e_s * 1e3,
-           "h2d_bytes_per_step": int(C_sizeof_uniforms()), "d2h_bytes_per_step": W * H * 4}
+           "h2d_bytes_per_step": int(C_sizeof_uniforms()), "d2h_bytes_per_step": W * H * 4,
+           "path": "vrt_render_to_host into page-locked host memory: the kernel's pixel stores cross the host "
+                   "link as it renders (no staging copy); uniforms go in as kernel parameters"}
 
     peak, peak_src = measured_peaks()
     algo_bytes = 4 * steps + 4 * hits + 4 * pixels

@@ -118,9 +118,10 @@ typedef struct vrt_render_opts {
     int32_t refill_min;      /* persistent kernel: lanes parked before a slow phase (0 = default) */
     int32_t blocks_per_sm;   /* persistent kernel: resident CTAs per SM it is built for (3 or 4) */
     int32_t exact_steps;     /* 1: count every DDA iteration of the shader, no early miss */
-    int32_t host_bands;      /* vrt_render_to_host with the tile kernel: the frame is rendered in this many
-                                bands of rows, each band's copy to the host overlapping the next band's
-                                render (0 = automatic, 1 = render then copy) */
+    int32_t host_bands;      /* vrt_render_to_host: 0 = automatic (page-locked memory is written by the
+                                kernel directly; other memory gets bands of 128 rows, up to 8); n > 0 =
+                                stage in device memory and copy, in n bands of rows with the tile kernel,
+                                each band's copy overlapping the next band's render (1 = render then copy) */
 } vrt_render_opts;
 
 typedef struct vrt_world vrt_world;
@@ -236,23 +237,28 @@ int vrt_renderer_create(vrt_renderer** out);
 int vrt_renderer_destroy(vrt_renderer* r);
 
 /* One frame: glDrawArrays(GL_TRIANGLES,0,6) over the fullscreen quad (main.cpp:59) with
- * the uniforms of render.cpp:289-296.  d_rgba: width*height*4 bytes, row 0 = bottom row
- * (GL order); pixel (px,py) sees vPos = ((2px+1)/width-1, (2py+1)/height-1).  dbg,
+ * the uniforms of render.cpp:289-296.  d_rgba: width*height*4 bytes, 4-byte aligned (one
+ * 32-bit store per pixel; VRT_EINVAL otherwise), any memory the device can store to, row
+ * 0 = bottom row (GL order); pixel (px,py) sees vPos = ((2px+1)/width-1, (2py+1)/height-1).  dbg,
  * d_stats and opts may be NULL.  The tile kernel's first render of a depth-field world
  * after its words changed also rebuilds the world's stop masks on this stream (allocated
  * on first use). */
 int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
                int32_t height, uint8_t* d_rgba, const vrt_debug_out* dbg, uint64_t* d_stats,
                const vrt_render_opts* opts, void* stream);
-/* vrt_render into the renderer's staging buffer and copy the image to host memory (pinned,
- * for the copies to run asynchronously).  With the tile kernel the frame is rendered in bands
- * of rows (vrt_render_opts.host_bands) and each band's copy runs on the renderer's copy
- * stream while the next band renders.  Waits for the image before returning. */
+/* vrt_render with the image in host memory; waits for the image before returning.
+ * - Page-locked host memory (vrt_host_alloc, cudaHostAlloc, cudaHostRegister; 4-byte
+ *   aligned) with host_bands = 0: the kernel stores each pixel straight into it over the
+ *   host link while it renders; nothing is staged or copied afterwards.
+ * - Otherwise (pageable memory, or host_bands > 0) the frame renders into the renderer's
+ *   staging buffer and is copied.  With the tile kernel it renders in bands of rows
+ *   (vrt_render_opts.host_bands), each band's copy running on the renderer's copy stream
+ *   while the next band renders. */
 int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
                        int32_t height, uint8_t* host_rgba, const vrt_render_opts* opts, void* stream);
 /* Page-locked host memory for images (cudaMallocHost), for callers without CUDA headers:
- * copies into it run asynchronously, which vrt_render_to_host's bands need to overlap the
- * render.  No counterpart in the reference.  vrt_host_free(NULL) is a no-op. */
+ * vrt_render_to_host's kernels store into it directly, and copies into it run
+ * asynchronously.  No counterpart in the reference.  vrt_host_free(NULL) is a no-op. */
 int vrt_host_alloc(size_t bytes, void** out);
 int vrt_host_free(void* p);
 

@@ -204,6 +204,38 @@ def test_render_to_host(cuda, small):
     assert np.array_equal(host.reshape(sc.height, sc.width, 4), g["rgba"])
 
 
+@pytest.mark.parametrize("kernel", KERNELS)
+def test_render_to_host_direct(cuda, small, kernel):
+    """Page-locked host memory is written by the kernel itself (no staging, no copy): the
+    image equals the device render's, also at an offset into the allocation.  A buffer
+    that is not 4-byte aligned goes through the staged copy; vrt_render refuses it."""
+    import torch
+    sc = small
+    width, height = 150, 90
+    u = sc.uniforms
+    u.aspectRatio = width / height
+    w = make_world(sc.words, sc.W, sc.H)
+    g = gpu_render(w, u, width, height, kernel=kernel)["rgba"]
+    n = width * height * 4
+    host = torch.zeros(n + 64, dtype=torch.uint8, pin_memory=True)
+    o = vrt.RenderOpts()
+    o.kernel = kernel
+    r = vrt.Renderer()
+    for off in (0, 16, 1, 3):  # 1 and 3: unaligned, staged
+        host.fill_(7)
+        r.render_to_host(w, u, width, height, host.data_ptr() + off, o)
+        out = host.numpy()
+        assert np.array_equal(out[off:off + n].reshape(height, width, 4), g), off
+        assert (out[:off] == 7).all() and (out[off + n:] == 7).all(), off  # nothing outside the image
+    with pytest.raises(vrt.VrtError) as e:
+        r.render(w, u, width, height, host.data_ptr() + 2, None, 0, o)
+    assert e.value.status == vrt.EINVAL
+    host.fill_(0)  # the device stores into page-locked memory through vrt_render too
+    r.render(w, u, width, height, host.data_ptr(), None, 0, o)
+    torch.cuda.synchronize()
+    assert np.array_equal(host.numpy()[:n].reshape(height, width, 4), g)
+
+
 @pytest.mark.parametrize("bands", [0, 1, 2, 3, 5, 8, 64])
 def test_render_to_host_in_bands(cuda, small, bands):
     """The banded host render (each band's copy overlapping the next band's render) gives

@@ -1292,6 +1292,8 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
                uint8_t* d_rgba, const vrt_debug_out* dbg, uint64_t* d_stats, const vrt_render_opts* opts,
                void* stream) {
     if (!r || !w || !d_rgba) return set_error(VRT_EINVAL, "NULL renderer, world or image");
+    if ((uintptr_t)d_rgba & 3)
+        return set_error(VRT_EINVAL, "image address not 4-byte aligned (one 32-bit store per pixel)");
     int st = check_uniforms(u);
     if (st) return st;
     if (width < 1 || height < 1 || width > 32768 || height > 32768)
@@ -1368,6 +1370,24 @@ int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* 
         return set_error(VRT_EINVAL, "image %d x %d out of range", width, height);
     int st = check_uniforms(u);
     if (st) return st;
+    const cudaStream_t s = S(stream);
+    if (!opts || opts->host_bands <= 0) {
+        // Page-locked host memory is mapped into the device's address space (unified
+        // addressing): the kernel stores the image into it over the host link as it renders,
+        // with no staging buffer and no copy after the render.
+        cudaPointerAttributes pa;
+        if (cudaPointerGetAttributes(&pa, host_rgba) != cudaSuccess) {
+            (void)cudaGetLastError();  // not a pointer the runtime knows: pageable memory
+            pa.type = cudaMemoryTypeUnregistered;
+        }
+        if (pa.type == cudaMemoryTypeHost && pa.devicePointer && ((uintptr_t)pa.devicePointer & 3) == 0) {
+            st = vrt_render(r, w, u, width, height, static_cast<uint8_t*>(pa.devicePointer), nullptr, nullptr, opts,
+                            stream);
+            if (st) return st;
+            VRT_CUDA(cudaStreamSynchronize(s));
+            return VRT_OK;
+        }
+    }
     size_t bytes = (size_t)width * height * 4;
     if (bytes > r->staging_bytes) {
         cudaFree(r->d_staging);
@@ -1377,7 +1397,6 @@ int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* 
         if (e != cudaSuccess) return set_error(VRT_ENOMEM, "staging image: %s", cudaGetErrorString(e));
         r->staging_bytes = bytes;
     }
-    const cudaStream_t s = S(stream);
     int kernel = opts ? opts->kernel : VRT_KERNEL_AUTO;
     if (kernel == VRT_KERNEL_AUTO && !w->has_depth_field) kernel = VRT_KERNEL_MASK_PIXEL;
     int bands = 1;
@@ -1446,8 +1465,9 @@ static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, st
     for (int i = 0; i < count; i++) {
         const vrt_view& v = views[i];
         if (v.world != w) return set_error(VRT_EINVAL, "view %d renders another world; one batch = one world", i);
-        if (!v.d_rgba || v.width < 1 || v.height < 1 || v.width > 32768 || v.height > 32768)
-            return set_error(VRT_EINVAL, "view %d: bad image", i);
+        if (!v.d_rgba || ((uintptr_t)v.d_rgba & 3) || v.width < 1 || v.height < 1 || v.width > 32768 ||
+            v.height > 32768)
+            return set_error(VRT_EINVAL, "view %d: bad image (NULL, not 4-byte aligned, or out of range)", i);
         int st = check_uniforms(&v.uniforms);
         if (st) return st;
         Tuning tv = t;  // a view may choose its own tile shape of the launch's tile size
@@ -1651,8 +1671,9 @@ extern "C" int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, co
     for (int i = 0; i < count; i++) {
         const vrt_view& v = views[i];
         if (v.world != w) return set_error(VRT_EINVAL, "view %d renders another world; one batch = one world", i);
-        if (!v.d_rgba || v.width < 1 || v.height < 1 || v.width > 32768 || v.height > 32768)
-            return set_error(VRT_EINVAL, "view %d: bad image", i);
+        if (!v.d_rgba || ((uintptr_t)v.d_rgba & 3) || v.width < 1 || v.height < 1 || v.width > 32768 ||
+            v.height > 32768)
+            return set_error(VRT_EINVAL, "view %d: bad image (NULL, not 4-byte aligned, or out of range)", i);
         st = check_uniforms(&v.uniforms);
         if (st) return st;
         Tuning tv = t;
