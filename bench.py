@@ -518,7 +518,8 @@ def bench_served(vrt, torch, scenes, sc, full_world):
     full_world.upload(sc.words)  # the served edits changed the shared world: restore it
     sat = max(x["mrays_per_s"] for x in results if "mrays_per_s" in x)
     return {"worlds": ["256x256x256", "512x256x512", "1024x256x1024", "1024x256x1024"], "budget_gib": 40,
-            "slots": 4, "max_batch": 8, "sweep": results,
+            "slots": 4, "max_batch": 8, "images": "page-locked host memory, stored by the render kernel",
+            "sweep": results,
             "plain_sync": {"renders": n_render, "seconds": plain_s, "mrays_per_s": plain_rays / plain_s / 1e6,
                            "ms_per_render": plain_s * 1e3 / max(n_render, 1)},
             "served_vs_plain_sync": sat / (plain_rays / plain_s / 1e6)}

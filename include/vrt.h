@@ -305,10 +305,15 @@ int vrt_batch_graph_destroy(vrt_batch_graph* g);
 /* ---- serving ---- */
 typedef struct vrt_server vrt_server;
 typedef struct vrt_server_config {
-    uint64_t memory_budget_bytes;   /* device bytes the server may hold for images (40 GiB) */
+    uint64_t memory_budget_bytes;   /* bytes the server may hold: its resident worlds' device
+                                       bytes plus the images of the requests in flight (40 GiB) */
     int32_t slots;                  /* concurrent batches in flight (streams)          */
     int32_t max_batch;              /* requests per launch                            */
-    int32_t max_wait_us;            /* how long a partial batch may wait for company   */
+    int32_t max_wait_us;            /* how long a partial batch may wait for company (0: none) */
+    int32_t image_memory;           /* where images render: 0 = page-locked host memory, stored
+                                       by the kernel (the request's own host_rgba when it is
+                                       page-locked and 4-byte aligned, else the slot's buffer);
+                                       1 = device memory, copied to the slot's host buffer */
 } vrt_server_config;
 
 #define VRT_REQ_RENDER 0
@@ -344,6 +349,10 @@ int vrt_server_submit(vrt_server* s, const vrt_request* req);
 int vrt_server_poll(vrt_server* s, vrt_completion* out, int32_t max_out);
 /* Run until every submitted request has completed (completions are kept for poll). */
 int vrt_server_drain(vrt_server* s);
+/* Wait, spinning on the slots' events, until a launch in flight has finished (returns 1:
+ * the next vrt_server_poll retires it), timeout_us passes or nothing is in flight
+ * (returns 0).  Call it from the thread that polls. */
+int vrt_server_wait(vrt_server* s, int32_t timeout_us);
 double vrt_server_now_ms(const vrt_server* s);
 
 /* ---- measurement helpers ---- */

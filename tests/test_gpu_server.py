@@ -13,8 +13,8 @@ from helpers import gpu_render, make_world
 pytestmark = pytest.mark.gpu
 
 
-def make_server(budget=1 << 30, slots=3, max_batch=4):
-    cfg = vrt.ServerConfig(budget, slots, max_batch, 0)
+def make_server(budget=1 << 30, slots=3, max_batch=4, max_wait_us=0, image_memory=0):
+    cfg = vrt.ServerConfig(budget, slots, max_batch, max_wait_us, image_memory)
     h = C.c_void_p()
     vrt.check(vrt.lib().vrt_server_create(C.byref(cfg), C.byref(h)))
     return h
@@ -32,7 +32,7 @@ def submit_render(srv, wid, u, width, height, out, tag):
     q.world_id = wid
     q.uniforms = u
     q.width, q.height = width, height
-    q.host_rgba = out.ctypes.data if out is not None else None
+    q.host_rgba = (out.ctypes.data if isinstance(out, np.ndarray) else out.data_ptr()) if out is not None else None
     q.user_tag = tag
     vrt.check(vrt.lib().vrt_server_submit(srv, C.byref(q)))
 
@@ -67,29 +67,42 @@ def worlds():
     return a, b
 
 
-def test_served_in_mix_equals_alone(cuda, worlds):
+def host_image(n, pinned):
+    """A result buffer: page-locked (the kernel stores into it) or pageable (copied)."""
+    if not pinned:
+        return np.zeros(n, np.uint8)
+    import torch
+    return torch.zeros(n, dtype=torch.uint8, pin_memory=True)
+
+
+def as_array(img):
+    return img if isinstance(img, np.ndarray) else img.numpy()
+
+
+@pytest.mark.parametrize("image_memory, pinned", [(0, False), (0, True), (1, False), (1, True)])
+def test_served_in_mix_equals_alone(cuda, worlds, image_memory, pinned):
+    """Images stored by the kernel into page-locked memory (the request's own buffer, or the
+    slot's and then copied to a pageable one), or rendered on the device and copied."""
     a, b = worlds
     wa, wb = make_world(a.words, a.W, a.H), make_world(b.words, b.W, b.H)
     views = scenes.batch_views(a, 10, seed=9, max_steps=256)
     views = [(u, w // 8 + 8, h // 8 + 6) for (u, w, h) in views]
-    srv = make_server()
+    srv = make_server(image_memory=image_memory)
     ia, ib = add_world(srv, wa), add_world(srv, wb)
     outs = {}
     for i, (u, w, h) in enumerate(views):
         u.aspectRatio = w / h
-        outs[i] = (np.zeros(w * h * 4, np.uint8), wa, u, w, h)
+        outs[i] = (host_image(w * h * 4, pinned), wa, u, w, h)
         submit_render(srv, ia, u, w, h, outs[i][0], i)
-        ub = b.uniforms
-        outs[100 + i] = (np.zeros(96 * 64 * 4, np.uint8), wb, ub, 96, 64)
-        ub2 = vrt.Uniforms.from_buffer_copy(ub)
+        ub2 = vrt.Uniforms.from_buffer_copy(b.uniforms)
         ub2.aspectRatio = 96 / 64
-        outs[100 + i] = (outs[100 + i][0], wb, ub2, 96, 64)
+        outs[100 + i] = (host_image(96 * 64 * 4, pinned), wb, ub2, 96, 64)
         submit_render(srv, ib, ub2, 96, 64, outs[100 + i][0], 100 + i)
     done = collect(srv, len(outs))
     for tag, (img, world, u, w, h) in outs.items():
         assert done[tag].status == 0
         alone = gpu_render(world, u, w, h)
-        assert np.array_equal(img.reshape(h, w, 4), alone["rgba"]), f"request {tag}"
+        assert np.array_equal(as_array(img).reshape(h, w, 4), alone["rgba"]), f"request {tag}"
         assert done[tag].rays == int(alone["stats"][vrt.STAT_RAYS])
         assert done[tag].done_ms >= done[tag].submit_ms
     vrt.lib().vrt_server_destroy(srv)
@@ -175,3 +188,43 @@ def test_depth_field_world_served(cuda, oracle, vrt_lib):
         o = oracle.render(stages[stage], W, H, u, 48, 32)
         assert np.array_equal(img.reshape(32, 48, 4), o["rgba"]), f"render {t} after {stage} edits"
     vrt.check(vrt.lib().vrt_server_destroy(srv))
+
+
+def test_partial_batch_waits_for_company(cuda, worlds):
+    """max_wait_us: a partial batch stays queued until it fills up (then it goes at once, as
+    one launch) or until its oldest request has waited max_wait_us."""
+    import time
+    _, b = worlds
+    w = make_world(b.words, b.W, b.H)
+    u = vrt.Uniforms.from_buffer_copy(b.uniforms)
+    u.aspectRatio = 1.0
+    alone = gpu_render(w, u, 32, 32)["rgba"]
+    srv = make_server(slots=2, max_batch=4, max_wait_us=2_000_000)
+    wid = add_world(srv, w)
+    imgs = [np.zeros(32 * 32 * 4, np.uint8) for _ in range(5)]
+    buf = (vrt.Completion * 16)()
+    for i in range(2):
+        submit_render(srv, wid, u, 32, 32, imgs[i], i)
+    assert vrt.check(vrt.lib().vrt_server_poll(srv, buf, 16)) == 0
+    assert vrt.check(vrt.lib().vrt_server_wait(srv, 1000)) == 0  # nothing in flight
+    for i in range(2, 4):
+        submit_render(srv, wid, u, 32, 32, imgs[i], i)
+    assert vrt.check(vrt.lib().vrt_server_poll(srv, buf, 16)) == 0  # launched, not done
+    assert vrt.check(vrt.lib().vrt_server_wait(srv, 5_000_000)) == 1
+    got = []
+    while len(got) < 4:
+        got += [buf[i] for i in range(vrt.check(vrt.lib().vrt_server_poll(srv, buf, 16)))]
+        if len(got) < 4:
+            vrt.check(vrt.lib().vrt_server_wait(srv, 100_000))
+    assert len({c.start_ms for c in got}) == 1  # one launch
+    vrt.lib().vrt_server_destroy(srv)
+    srv = make_server(slots=2, max_batch=4, max_wait_us=30_000)
+    wid = add_world(srv, w)
+    submit_render(srv, wid, u, 32, 32, imgs[4], 4)
+    t0 = time.perf_counter()
+    done = collect(srv, 1)
+    assert time.perf_counter() - t0 >= 0.025
+    assert done[4].start_ms - done[4].submit_ms >= 29.0
+    for img in imgs:
+        assert np.array_equal(img.reshape(32, 32, 4), alone)
+    vrt.lib().vrt_server_destroy(srv)

@@ -5,13 +5,16 @@
 // (vrt_server_submit, thread-safe) and vrt_server_poll:
 //   - retires finished launches (event query, never blocks) and frees their images;
 //   - admits queued requests into free slots (a slot = a stream + a renderer) while the
-//     device memory budget (resident worlds + images in flight) allows;
-//   - batches the renders of one world into one persistent launch (vrt_render_batch),
-//     so requests that arrive while others run join the next free slot and overlap them
-//     on the device;
+//     memory budget (resident worlds + images in flight) allows;
+//   - batches the renders of one world into one launch (vrt_render_batch), so requests
+//     that arrive while others run join the next free slot and overlap them on the device;
+//     a partial batch may wait max_wait_us for company;
 //   - keeps the order of each world's requests: an edit waits (on the device, through
 //     events) for every earlier render of its world, and later renders wait for it.
 // Requests larger than the whole budget complete with VRT_EBUDGET.
+// Images render straight into page-locked host memory by default (the kernels store the
+// pixels over the host link): the request's own buffer when it is page-locked, else the
+// slot's.  image_memory = 1 renders into device memory and copies to the slot's buffer.
 #include <cuda_runtime.h>
 
 #include <algorithm>
@@ -19,6 +22,7 @@
 #include <cstring>
 #include <deque>
 #include <mutex>
+#include <thread>
 #include <vector>
 
 #include "vrt_internal.h"
@@ -30,7 +34,7 @@ using Clock = std::chrono::steady_clock;
 struct Queued {
     vrt_request req;
     double submit_ms;
-    uint64_t bytes;  // device image bytes (render)
+    uint64_t bytes;  // image bytes (render)
 };
 
 struct WorldEntry {
@@ -47,12 +51,14 @@ struct Slot {
     int world_id = -1;
     bool is_edit = false;
     std::vector<Queued> reqs;
-    std::vector<uint8_t*> d_images;
+    std::vector<uint8_t*> d_images;   // device images (image_memory = 1), else NULL
     std::vector<uint64_t> image_bytes;
+    std::vector<char> in_place;       // rendered straight into the request's own buffer
     uint64_t* d_stats = nullptr;  // per request VRT_STAT_COUNT counters
     uint64_t* h_stats = nullptr;  // pinned
     int stats_cap = 0;
     uint8_t* h_staging = nullptr;  // pinned
+    uint8_t* staging_dev = nullptr;  // h_staging's address in the device's address space
     uint64_t staging_cap = 0;
     double start_ms = 0;
     uint64_t bytes_in_flight = 0;
@@ -112,12 +118,12 @@ static void retire(vrt_server* s, Slot& sl) {
         c.done_ms = t;
         if (q.req.kind == VRT_REQ_RENDER) {
             c.rays = sl.h_stats[i * VRT_STAT_COUNT + VRT_STAT_RAYS];
-            if (q.req.host_rgba) {
+            if (q.req.host_rgba && !sl.in_place[i]) {
                 uint64_t off = 0;
                 for (size_t j = 0; j < i; j++) off += sl.image_bytes[j];
                 std::memcpy(q.req.host_rgba, sl.h_staging + off, sl.image_bytes[i]);
             }
-            s->pool.put(sl.image_bytes[i], sl.d_images[i]);
+            if (sl.d_images[i]) s->pool.put(sl.image_bytes[i], sl.d_images[i]);
         }
         s->done.push_back(c);
     }
@@ -126,6 +132,7 @@ static void retire(vrt_server* s, Slot& sl) {
     sl.reqs.clear();
     sl.d_images.clear();
     sl.image_bytes.clear();
+    sl.in_place.clear();
     sl.busy = false;
 }
 
@@ -174,50 +181,90 @@ static int ensure_slot_buffers(Slot& sl, int n, uint64_t bytes) {
         sl.h_staging = nullptr;
         sl.staging_cap = 0;
         VRT_CUDA(cudaMallocHost(&sl.h_staging, bytes));
+        void* dev = nullptr;
+        VRT_CUDA(cudaHostGetDevicePointer(&dev, sl.h_staging, 0));
+        sl.staging_dev = static_cast<uint8_t*>(dev);
         sl.staging_cap = bytes;
     }
     return VRT_OK;
+}
+
+// The address the kernel can store a request's image to when the request's own buffer is
+// page-locked host memory (mapped into the device's address space), else NULL.
+static uint8_t* mapped_host_image(uint8_t* host) {
+    if (!host) return nullptr;
+    cudaPointerAttributes pa;
+    if (cudaPointerGetAttributes(&pa, host) != cudaSuccess) {
+        (void)cudaGetLastError();  // pageable memory
+        return nullptr;
+    }
+    if (pa.type != cudaMemoryTypeHost || !pa.devicePointer || ((uintptr_t)pa.devicePointer & 3)) return nullptr;
+    return static_cast<uint8_t*>(pa.devicePointer);
+}
+
+static void release_images(vrt_server* s, Slot& sl) {
+    for (size_t i = 0; i < sl.d_images.size(); i++)
+        if (sl.d_images[i]) s->pool.put(sl.image_bytes[i], sl.d_images[i]);
+    sl.d_images.clear();
+    sl.image_bytes.clear();
+    sl.in_place.clear();
 }
 
 static int launch_renders(vrt_server* s, int si, std::vector<Queued>& batch) {
     Slot& sl = s->slots[si];
     const int wid = batch[0].req.world_id;
     WorldEntry& we = s->worlds[wid];
+    const bool on_device = s->cfg.image_memory == 1;
     uint64_t total = 0;
     for (auto& q : batch) total += q.bytes;
     int st = ensure_slot_buffers(sl, (int)batch.size(), total);
     if (st) return st;
     std::vector<vrt_view> views(batch.size());
-    sl.d_images.clear();
-    sl.image_bytes.clear();
+    release_images(s, sl);
+    uint64_t off = 0;
     for (size_t i = 0; i < batch.size(); i++) {
-        uint8_t* img = s->pool.get(batch[i].bytes);
-        if (!img) {
-            for (size_t j = 0; j < i; j++) s->pool.put(sl.image_bytes[j], sl.d_images[j]);
-            sl.d_images.clear();
-            sl.image_bytes.clear();
-            return set_error(VRT_ENOMEM, "image allocation failed");
+        uint8_t* img = nullptr;
+        uint8_t* dst = nullptr;
+        bool in_place = false;
+        if (on_device) {
+            img = s->pool.get(batch[i].bytes);
+            if (!img) {
+                release_images(s, sl);
+                return set_error(VRT_ENOMEM, "image allocation failed");
+            }
+            dst = img;
+        } else {
+            dst = mapped_host_image(batch[i].req.host_rgba);
+            in_place = dst != nullptr;
+            if (!dst) dst = sl.staging_dev + off;  // image bytes are multiples of 4: aligned
         }
+        off += batch[i].bytes;
         sl.d_images.push_back(img);
         sl.image_bytes.push_back(batch[i].bytes);
+        sl.in_place.push_back(in_place);
         vrt_view& v = views[i];
         std::memset(&v, 0, sizeof(v));
         v.world = we.w;
         v.uniforms = batch[i].req.uniforms;
         v.width = batch[i].req.width;
         v.height = batch[i].req.height;
-        v.d_rgba = img;
+        v.d_rgba = dst;
         v.d_stats = sl.d_stats + i * VRT_STAT_COUNT;
     }
     if (we.has_edit) VRT_CUDA(cudaStreamWaitEvent(sl.stream, we.edit_event, 0));
     VRT_CUDA(cudaMemsetAsync(sl.d_stats, 0, sizeof(uint64_t) * VRT_STAT_COUNT * batch.size(), sl.stream));
     st = vrt_render_batch(sl.renderer, views.data(), (int)views.size(), nullptr, sl.stream);
-    if (st) return st;
-    uint64_t off = 0;
-    for (size_t i = 0; i < batch.size(); i++) {
-        VRT_CUDA(cudaMemcpyAsync(sl.h_staging + off, sl.d_images[i], sl.image_bytes[i], cudaMemcpyDeviceToHost,
-                                 sl.stream));
-        off += sl.image_bytes[i];
+    if (st) {
+        release_images(s, sl);
+        return st;
+    }
+    if (on_device) {
+        off = 0;
+        for (size_t i = 0; i < batch.size(); i++) {
+            VRT_CUDA(cudaMemcpyAsync(sl.h_staging + off, sl.d_images[i], sl.image_bytes[i], cudaMemcpyDeviceToHost,
+                                     sl.stream));
+            off += sl.image_bytes[i];
+        }
     }
     VRT_CUDA(cudaMemcpyAsync(sl.h_stats, sl.d_stats, sizeof(uint64_t) * VRT_STAT_COUNT * batch.size(),
                              cudaMemcpyDeviceToHost, sl.stream));
@@ -256,6 +303,24 @@ static bool admit(vrt_server* s, int si, int* status) {
             if (s->image_bytes + it->bytes > cap) {
                 blocked[wid] = 1;
                 continue;
+            }
+            if (s->cfg.max_wait_us > 0 && s->now() - it->submit_ms < 1e-3 * s->cfg.max_wait_us) {
+                // a young partial batch waits for company (a full one, or one that meets the
+                // world's next edit, goes now)
+                int n = 0;
+                bool closed = false;
+                for (auto jt = it; jt != s->queue.end() && n < s->cfg.max_batch; ++jt) {
+                    if (jt->req.world_id != wid) continue;
+                    if (jt->req.kind == VRT_REQ_EDIT) {
+                        closed = true;
+                        break;
+                    }
+                    n++;
+                }
+                if (n < s->cfg.max_batch && !closed) {
+                    blocked[wid] = 1;
+                    continue;
+                }
             }
             // gather this world's renders in order, up to the first edit of the world
             uint64_t used = s->image_bytes;
@@ -313,7 +378,7 @@ int vrt_server_destroy(vrt_server* s) {
     if (!s) return VRT_OK;
     for (auto& sl : s->slots) {
         if (sl.stream) cudaStreamSynchronize(sl.stream);
-        for (size_t i = 0; i < sl.d_images.size(); i++) s->pool.put(sl.image_bytes[i], sl.d_images[i]);
+        release_images(s, sl);
         vrt_renderer_destroy(sl.renderer);
         if (sl.done) cudaEventDestroy(sl.done);
         if (sl.stream) cudaStreamDestroy(sl.stream);
@@ -420,6 +485,23 @@ int vrt_server_drain(vrt_server* s) {
                     break;
                 }
         }
+    }
+}
+
+int vrt_server_wait(vrt_server* s, int32_t timeout_us) {
+    if (!s) return set_error(VRT_EINVAL, "NULL server");
+    const Clock::time_point end = Clock::now() + std::chrono::microseconds(std::max(0, timeout_us));
+    for (;;) {
+        bool busy = false;
+        for (auto& sl : s->slots) {
+            if (!sl.busy) continue;
+            busy = true;
+            const cudaError_t e = cudaEventQuery(sl.done);
+            if (e == cudaSuccess) return 1;
+            if (e != cudaErrorNotReady) return cuda_error(e, "slot event");
+        }
+        if (!busy || Clock::now() >= end) return 0;
+        std::this_thread::yield();
     }
 }
 

@@ -4,8 +4,9 @@ and edit requests over resident worlds, latency percentiles and throughput.
 Requests: 90% renders at 640x360, 1280x720 or 1920x1080 with a random surface camera
 and 0-16 of the world's lights; 10% edits that remove a sphere of radius 1-8 at a
 surface point (removeSphere, level.cpp:30-56).  Arrivals are generated on the host
-clock and submitted when due; vrt_server_poll is called in between, so requests that
-arrive while others run are admitted as slots and memory free up.
+clock and submitted when due; in between, the driver waits on the server
+(vrt_server_wait: until a launch finishes or the next arrival is due) and polls, so
+requests that arrive while others run are admitted as slots and memory free up.
 """
 from __future__ import annotations
 
@@ -22,8 +23,9 @@ RESOLUTIONS = [(640, 360), (1280, 720), (1920, 1080)]
 
 
 class Server:
-    def __init__(self, budget_bytes: int, slots: int = 4, max_batch: int = 8, max_wait_us: int = 0):
-        cfg = vrt.ServerConfig(budget_bytes, slots, max_batch, max_wait_us)
+    def __init__(self, budget_bytes: int, slots: int = 4, max_batch: int = 8, max_wait_us: int = 0,
+                 image_memory: int = 0):
+        cfg = vrt.ServerConfig(budget_bytes, slots, max_batch, max_wait_us, image_memory)
         self.h = C.c_void_p()
         vrt.check(vrt.lib().vrt_server_create(C.byref(cfg), C.byref(self.h)))
         self._buf = (vrt.Completion * 512)()
@@ -48,6 +50,10 @@ class Server:
             if not got:
                 return out
             out += got
+
+    def wait(self, timeout_us: int) -> bool:
+        """True when a launch in flight has finished (poll retires it)."""
+        return vrt.check(vrt.lib().vrt_server_wait(self.h, int(timeout_us))) == 1
 
     def now_ms(self) -> float:
         return vrt.lib().vrt_server_now_ms(self.h)
@@ -116,8 +122,12 @@ def run_open_loop(server: Server, wids, requests, keep_images: bool = False):
         done += server.poll()
         if i < n:
             wait = requests[i][0] - (time.perf_counter() - t0)
-            if wait > 0.0005:
-                time.sleep(min(wait, 0.0005))
+            # until a launch finishes or the next request is due; with nothing in flight,
+            # sleep in short steps (a late wake-up then stays small)
+            if wait > 0 and not server.wait(min(wait, 0.002) * 1e6):
+                left = requests[i][0] - (time.perf_counter() - t0)
+                if left > 0.0002:
+                    time.sleep(min(left - 0.0001, 0.0005))
     done += server.drain()
     wall = time.perf_counter() - t0
     return done, wall

@@ -114,6 +114,7 @@ class ServerConfig(C.Structure):
         ("slots", C.c_int32),
         ("max_batch", C.c_int32),
         ("max_wait_us", C.c_int32),
+        ("image_memory", C.c_int32),
     ]
 
 
@@ -194,6 +195,7 @@ SIGNATURES = {
     "vrt_server_submit": (_I, [_P, C.POINTER(Request)]),
     "vrt_server_poll": (_I, [_P, C.POINTER(Completion), _I]),
     "vrt_server_drain": (_I, [_P]),
+    "vrt_server_wait": (_I, [_P, _I]),
     "vrt_server_now_ms": (C.c_double, [_P]),
     "vrt_probe_l2_read_gbs": (_I, [_U64, _I, C.POINTER(C.c_double)]),
 }
