@@ -420,8 +420,8 @@ def bench_batched(vrt, torch, scenes, sc, world, r, dev, stream):
             "plain_sync_ms": sync_ms, "plain_sync_mrays_per_s": rays / (sync_ms * 1e-3) / 1e6,
             "speedup_vs_sync": sync_ms / batched_ms,
             "note": "plain = one vrt_render launch per camera, back to back on one stream; plain_sync = "
-                    "vrt_render_to_host per camera (render, copy the image to host, wait) -- the batched "
-                    "result is compared without its copies",
+                    "vrt_render_to_host per camera (render into page-locked host memory, wait) -- the "
+                    "batched result stays in device memory",
             "autotuned": plan.describe(), "autotune_best": top}
 
 
