@@ -30,9 +30,10 @@ def test_reference_scene(cuda, oracle):
     assert (col.view(np.uint32) == case["color_bits"][:, :3]).all()
     o = oracle.render(words, 512, 96, u, 800, 600)
     assert_same_frame(o, g)
-    f = gpu_render(w, u, 800, 600, kernel=vrt.KERNEL_MASK_PIXEL, debug=False)  # inexact launch
-    assert np.array_equal(f["rgba"], o["rgba"])
-    assert int(f["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"]
+    for k in (vrt.KERNEL_MASK_PIXEL, vrt.KERNEL_WORD):  # inexact launches
+        f = gpu_render(w, u, 800, 600, kernel=k, debug=False)
+        assert np.array_equal(f["rgba"], o["rgba"]), k
+        assert int(f["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"]
 
 
 def test_edits_refresh_the_stop_masks(cuda, oracle, vrt_lib):
@@ -67,8 +68,9 @@ def test_random_depth_field_scenes(cuda, oracle, seed):
             assert_same_frame(o, gpu_render(w, u, width, height, kernel=k))
         except AssertionError as e:
             raise AssertionError(f"seed {seed}, kernel {k}: {e}") from None
-    g = gpu_render(w, u, width, height, kernel=vrt.KERNEL_MASK_PIXEL, debug=False)
-    assert np.array_equal(o["rgba"], g["rgba"]), f"seed {seed}: inexact launch"
+    for k in (vrt.KERNEL_MASK_PIXEL, vrt.KERNEL_WORD):
+        g = gpu_render(w, u, width, height, kernel=k, debug=False)
+        assert np.array_equal(o["rgba"], g["rgba"]), f"seed {seed}, kernel {k}: inexact launch"
 
 
 def test_batch_on_a_depth_field_world(cuda, oracle):

@@ -1,5 +1,6 @@
 """Randomised parity: random worlds, cameras, lights, radii, overbright limits and step
-caps; every render kernel (and the tile kernel's inexact launch) against the oracle.
+caps; every render kernel (and the inexact launches of the tile and word kernels)
+against the oracle.
 
 Each case is seeded, so a failure names a reproducible scene."""
 import math
@@ -75,6 +76,7 @@ def test_random_scene(cuda, oracle, seed):
             assert_same_frame(o, gpu_render(world, u, width, height, kernel=k))
         except AssertionError as e:
             raise AssertionError(f"seed {seed}, kernel {k}: {e}") from None
-    g = gpu_render(world, u, width, height, kernel=vrt.KERNEL_MASK_PIXEL, debug=False)
-    assert np.array_equal(o["rgba"], g["rgba"]), f"seed {seed}: inexact launch"
-    assert int(g["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"]
+    for k in (vrt.KERNEL_MASK_PIXEL, vrt.KERNEL_WORD):  # inexact launches: rays that cannot hit end early
+        g = gpu_render(world, u, width, height, kernel=k, debug=False)
+        assert np.array_equal(o["rgba"], g["rgba"]), f"seed {seed}, kernel {k}: inexact launch"
+        assert int(g["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"]

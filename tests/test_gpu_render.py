@@ -70,8 +70,8 @@ def test_full_world_reduced_frame(cuda, oracle, full_world, kernel):
 
 @pytest.mark.parametrize("kernel", KERNELS)
 def test_fast_mode_images_are_exact(cuda, oracle, full_world, kernel):
-    """Without step outputs the mask kernels end rays that cannot hit early: the image,
-    rays, hits and pixels stay exactly the oracle's; with exact_steps the steps do too."""
+    """Without step outputs every kernel ends rays that cannot hit early: the image, rays,
+    hits and pixels stay exactly the oracle's; with exact_steps the steps do too."""
     sc = full_world
     o = oracle.render(sc.words, sc.W, sc.H, sc.uniforms, 480, 270)
     w = make_world(sc.words, sc.W, sc.H)
@@ -79,8 +79,7 @@ def test_fast_mode_images_are_exact(cuda, oracle, full_world, kernel):
     assert np.array_equal(g["rgba"], o["rgba"])
     t = o["totals"]
     assert [int(v) for v in g["stats"][[0, 2, 3]]] == [t["rays"], t["hits"], t["pixels"]]
-    if kernel != vrt.KERNEL_WORD:
-        assert int(g["stats"][vrt.STAT_STEPS]) < t["steps"]  # rays that cannot hit ended early
+    assert int(g["stats"][vrt.STAT_STEPS]) < t["steps"]  # rays that cannot hit ended early
     e = gpu_render(w, sc.uniforms, 480, 270, kernel=kernel, debug=False, exact_steps=1)
     assert np.array_equal(e["rgba"], o["rgba"]) and int(e["stats"][vrt.STAT_STEPS]) == t["steps"]
 

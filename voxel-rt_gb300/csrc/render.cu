@@ -35,6 +35,8 @@ struct WordParams {
     uint8_t* rgba;
     vrt_debug_out dbg;
     unsigned long long* stats;
+    int bb[6];   // solid bounding box: min x,y,z, max x,y,z (never smaller than the truth)
+    int exact;   // 1: every DDA iteration of the shader runs (step counts asked for)
 };
 
 // fl(i / 255) for i = 0..255: the shader's channel scale (fshader.glsl:184-186), filled on
@@ -95,13 +97,28 @@ struct WordRay {
     int steps;
 };
 
-// castRay, fshader.glsl:59-129, over the voxel words.
-__device__ WordRay cast_word(const int32_t* __restrict__ words, const Layout& L, V3 start, V3 dir, int dist,
-                             int maxSteps) {
+// castRay, fshader.glsl:59-129, over the voxel words.  A cell outside the world ends the
+// ray, getVoxelIndex == -1 (:123-125).  Inexact launches also end a ray that cannot hit
+// anything: a cell in [lo_y, lo_y + span_y) along y stays alive, beyond the solid box the
+// ray moves away from (or does not move along) along y ends it, since every later cell
+// stays beyond it.  Depth-field jumps move the start forward along dir, so they keep that
+// true.  (Only y: in terrain worlds the solid box spans x and z, and two registers per
+// ray are what this latency-bound kernel can spare.)
+__device__ WordRay cast_word(const int32_t* __restrict__ words, const Layout& L, const WordParams& p, V3 start,
+                             V3 dir, int dist, int maxSteps) {
     WordRay o;
     o.hit = -1; o.cd = 0.0f; o.axis = 2; o.s = 0; o.steps = 0;
     RaySetup r;
     ray_setup(start, dir, r);
+    int lo_y = 0, span_y = L.H;
+    if (!p.exact) {
+        if (r.sy > 0) {
+            span_y = max(0, min(L.H, p.bb[4] + 1));
+        } else {
+            lo_y = min(max(0, p.bb[1]), L.H);
+            span_y = L.H - lo_y;
+        }
+    }
     float cd = 0.0f, travelled = 0.0f;
     const float fdist = (float)dist, fcap = (float)maxSteps;
     int axis = 2, s = 0;
@@ -115,8 +132,9 @@ __device__ WordRay cast_word(const int32_t* __restrict__ words, const Layout& L,
         } else {
             cd = r.tz; r.cz += r.sz; r.tz = fadd(r.tz, r.dz); axis = 2; s = r.sz;
         }
-        if ((unsigned)r.cx >= (unsigned)L.W || (unsigned)r.cy >= (unsigned)L.H || (unsigned)r.cz >= (unsigned)L.W)
-            break;  // getVoxelIndex == -1
+        if ((unsigned)r.cx >= (unsigned)L.W || (unsigned)(r.cy - lo_y) >= (unsigned)span_y ||
+            (unsigned)r.cz >= (unsigned)L.W)
+            break;  // getVoxelIndex == -1, or no solid voxel ahead
         int32_t idx = r.cx + L.W * r.cy + L.W * L.H * r.cz;
         int32_t v = __ldg(words + idx);
         if (v >= 0) {
@@ -151,7 +169,7 @@ __global__ void __launch_bounds__(128) render_word_kernel(const int32_t* __restr
     pr.hit = -1; pr.cd = 0.f; pr.axis = 2; pr.s = 0; pr.start = cam; pr.steps = 0;
     if (valid) {
         rd = primary_dir(u, px, py, p.width, p.height);
-        pr = cast_word(words, L, cam, rd, u.maxSteps, u.maxSteps);
+        pr = cast_word(words, L, p, cam, rd, u.maxSteps, u.maxSteps);
     }
     const bool lit = valid && pr.hit >= 0 && u.viewDepthField != 1;
     const V3 hp = lit ? add3(mul3s(rd, pr.cd), pr.start) : V3{0.f, 0.f, 0.f};
@@ -168,7 +186,7 @@ __global__ void __launch_bounds__(128) render_word_kernel(const int32_t* __restr
             V3 hn = axis_normal(pr.axis, pr.s);
             V3 lp{u.lightPos[0], u.lightPos[1], u.lightPos[2]};
             V3 toLight = norm3(sub3(lp, hp));
-            WordRay sr = cast_word(words, L, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps, u.maxSteps);
+            WordRay sr = cast_word(words, L, p, add3(hp, mul3s(toLight, 0.001f)), toLight, u.maxSteps, u.maxSteps);
             res.steps += sr.steps;
             res.cast |= 1u;
             if (sr.hit < 0) {
@@ -200,7 +218,7 @@ __global__ void __launch_bounds__(128) render_word_kernel(const int32_t* __restr
                 float ld = len3(dl);
                 if (ld <= R) {
                     V3 tl = norm3(dl);
-                    WordRay lr = cast_word(words, L, add3(hp, mul3s(tl, 0.001f)), tl, f2i(fadd(ld, 1.0f)),
+                    WordRay lr = cast_word(words, L, p, add3(hp, mul3s(tl, 0.001f)), tl, f2i(fadd(ld, 1.0f)),
                                            u.maxSteps);
                     res.steps += lr.steps;
                     res.cast |= 2u << i;
@@ -1311,6 +1329,8 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
         p.rgba = d_rgba;
         if (dbg) p.dbg = *dbg;
         p.stats = reinterpret_cast<unsigned long long*>(d_stats);
+        std::memcpy(p.bb, w->h_aabb, sizeof(p.bb));
+        p.exact = (opts && opts->exact_steps) || u->viewDepthField == 1 || (dbg && (dbg->steps || dbg->primary_steps));
         dim3 grid((width + 15) / 16, (height + 7) / 8);
         const bool debug = dbg && (dbg->hit_index || dbg->cast_mask || dbg->occ_mask || dbg->steps ||
                                    dbg->primary_steps || dbg->shade);
