@@ -114,7 +114,8 @@ typedef struct vrt_debug_out {
  * asked for: exact_steps = 1, a steps or primary_steps debug output, or viewDepthField. */
 typedef struct vrt_render_opts {
     int32_t kernel;          /* VRT_KERNEL_*                                        */
-    int32_t tile_w, tile_h;  /* ray tile (0 = kernel default: 8x16 tile kernel, 8x4 persistent) */
+    int32_t tile_w, tile_h;  /* ray tile (0 = kernel default: 8x16 tile kernel, 8x4 persistent, 16x8 word
+                                kernel); tile and word kernels: tile_w*tile_h a multiple of 32, at most 128 */
     int32_t refill_min;      /* persistent kernel: lanes parked before a slow phase (0 = default) */
     int32_t blocks_per_sm;   /* persistent kernel: resident CTAs per SM it is built for (3 or 4) */
     int32_t exact_steps;     /* 1: count every DDA iteration of the shader, no early miss */

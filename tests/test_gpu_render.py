@@ -160,6 +160,18 @@ def test_tile_kernel_tile_shapes_are_invisible(cuda, oracle, full_world):
         gpu_render(w, u, 16, 16, kernel=vrt.KERNEL_MASK_PIXEL, tile=(5, 3))
 
 
+def test_word_kernel_pixel_tiles_are_invisible(cuda, oracle, full_world):
+    sc = full_world
+    u = sc.uniforms
+    o = oracle.render(sc.words, sc.W, sc.H, u, 200, 113)
+    w = make_world(sc.words, sc.W, sc.H)
+    for tile in [(16, 8), (8, 4), (32, 1), (1, 32), (16, 4), (64, 2), (96, 1)]:
+        assert_same_frame(o, gpu_render(w, u, 200, 113, kernel=vrt.KERNEL_WORD, tile=tile))
+    for bad in [(5, 3), (16, 16)]:
+        with pytest.raises(vrt.VrtError):
+            gpu_render(w, u, 16, 16, kernel=vrt.KERNEL_WORD, tile=bad)
+
+
 @pytest.mark.parametrize("dims", [(37, 21), (70, 65), (130, 8)])
 def test_odd_world_sizes_random_voxels(cuda, oracle, dims):
     """World sizes that are not multiples of the brick/region/super sizes, dense noise."""

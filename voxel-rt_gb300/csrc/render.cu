@@ -37,6 +37,7 @@ struct WordParams {
     unsigned long long* stats;
     int bb[6];   // solid bounding box: min x,y,z, max x,y,z (never smaller than the truth)
     int exact;   // 1: every DDA iteration of the shader runs (step counts asked for)
+    int tw, th;  // pixel tile of a CTA (tw * th threads)
 };
 
 // fl(i / 255) for i = 0..255: the shader's channel scale (fshader.glsl:184-186), filled on
@@ -158,8 +159,8 @@ __device__ WordRay cast_word(const int32_t* __restrict__ words, const Layout& L,
 template <bool DEBUG>
 __global__ void __launch_bounds__(128) render_word_kernel(const int32_t* __restrict__ words, Layout L,
                                                           const __grid_constant__ WordParams p) {
-    const int px = blockIdx.x * 16 + (threadIdx.x & 15);
-    const int py = blockIdx.y * 8 + (threadIdx.x >> 4);
+    const int px = blockIdx.x * p.tw + (int)threadIdx.x % p.tw;
+    const int py = blockIdx.y * p.th + (int)threadIdx.x / p.tw;
     const bool valid = px < p.width && py < p.height;
     PixelResult res{};
     const vrt_uniforms& u = p.u;
@@ -1331,11 +1332,18 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
         p.stats = reinterpret_cast<unsigned long long*>(d_stats);
         std::memcpy(p.bb, w->h_aabb, sizeof(p.bb));
         p.exact = (opts && opts->exact_steps) || u->viewDepthField == 1 || (dbg && (dbg->steps || dbg->primary_steps));
-        dim3 grid((width + 15) / 16, (height + 7) / 8);
+        // 16x8 pixels per CTA unless the options name another tile (a multiple of 32 threads, at most 128)
+        p.tw = opts && opts->tile_w > 0 && opts->tile_h > 0 ? opts->tile_w : 16;
+        p.th = opts && opts->tile_w > 0 && opts->tile_h > 0 ? opts->tile_h : 8;
+        const int threads = p.tw * p.th;
+        if (threads % 32 != 0 || threads > 128)
+            return set_error(VRT_EINVAL, "pixel tile %dx%d: tile_w*tile_h must be a multiple of 32 up to 128", p.tw,
+                             p.th);
+        dim3 grid((width + p.tw - 1) / p.tw, (height + p.th - 1) / p.th);
         const bool debug = dbg && (dbg->hit_index || dbg->cast_mask || dbg->occ_mask || dbg->steps ||
                                    dbg->primary_steps || dbg->shade);
-        if (debug) render_word_kernel<true><<<grid, 128, 0, S(stream)>>>(w->d_words, w->L, p);
-        else render_word_kernel<false><<<grid, 128, 0, S(stream)>>>(w->d_words, w->L, p);
+        if (debug) render_word_kernel<true><<<grid, threads, 0, S(stream)>>>(w->d_words, w->L, p);
+        else render_word_kernel<false><<<grid, threads, 0, S(stream)>>>(w->d_words, w->L, p);
         VRT_CUDA(cudaGetLastError());
         return VRT_OK;
     }
