@@ -106,6 +106,26 @@ class ClockSampler:
                 "samples": len(sm)}
 
 
+def cpu_model() -> str:
+    """The host CPU's model name (lscpu, else /proc/cpuinfo, else the machine type)."""
+    import platform
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.lower().startswith("model name"):
+                return line.split(":", 1)[1].strip()
+    except (OSError, subprocess.SubprocessError):
+        pass
+    try:
+        with open("/proc/cpuinfo") as f:
+            for line in f:
+                if line.lower().startswith("model name"):
+                    return line.split(":", 1)[1].strip()
+    except OSError:
+        pass
+    return platform.machine()
+
+
 def cpu_baseline(scene, target_s: float, threads: int):
     """Oracle (-O3, no contraction, OpenMP over rows) on the same frame: whole frames
     repeated until about target_s of CPU time, or an even row sample when one frame
@@ -130,7 +150,7 @@ def cpu_baseline(scene, target_s: float, threads: int):
     nrows = len(range(0, scene.height, stride))
     what = (f"{reps} whole {scene.width}x{scene.height} frames" if stride == 1 else
             f"every {stride}th row of the {scene.width}x{scene.height} frame ({nrows} rows)")
-    return {"value": rays / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port",
+    return {"value": rays / dt / 1e6, "unit": UNIT, "cores": threads, "kind": "port", "cpu": cpu_model(),
             "sample": f"{what}: {rays} rays in {dt:.2f} s", "seconds": dt / reps}
 
 
@@ -153,7 +173,7 @@ def run_reference(args):
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded terrain)",
         "config": {"workload": sc.workload, "sample": steps[-1]["sample"]},
-        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port",
+        "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port", "cpu": steps[-1]["cpu"],
                          "sample": steps[-1]["sample"]},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "note": "the reference path is a GLSL fragment shader (no graphics stack here); its CPU restatement "
