@@ -695,17 +695,20 @@ struct BoxRay {
     int ex, ey, ez;
     int sx, sy, sz;
     uint32_t oct;    // octant of travel: bit a set when s_a > 0
-    int left;        // DDA iterations left after the current one: negative on the last allowed one
+    int lb;          // lb + kx + ky + kz = DDA iterations left after the current one (negative on
+                     // the last allowed one): every iteration lowers exactly one k
     int bi;          // bit of the current cell in m (valid while m != 0)
     uint64_t m;      // voxel bits of the current brick, 0 inside an empty box
 };
 
-__device__ __forceinline__ void set_axis(int c, int s, int lo, int hi, int& k, int& e) {
-    // e is the first cell past the far face; k = s * (e - c) - 1 is one multiply-add,
-    // which issues on the FMA pipe rather than the integer/logic pipe
+// kmax limits k: a box is cut short so that the ray leaves it by its last allowed
+// iteration (see cast_box).  e = c + s * (k + 1) is the first cell past the (possibly
+// nearer) far face; k = s * (ee - c) - 1 and e are multiply-adds, which issue on the FMA
+// pipe rather than the integer/logic pipe.
+__device__ __forceinline__ void set_axis(int c, int s, int lo, int hi, int kmax, int& k, int& e) {
     const int ee = s > 0 ? hi : lo - 1;
-    k = s != 0 ? s * (ee - c) - 1 : INT_MAX;
-    e = s != 0 ? ee : c;
+    k = min(s != 0 ? s * (ee - c) - 1 : INT_MAX, kmax);
+    e = s * (k + 1) + c;
 }
 
 // Per-octant alive ranges of a launch, one (lo, span) pair per octant and axis: a cell
@@ -739,9 +742,12 @@ __device__ __forceinline__ void fill_alive_ranges(int2* alive, const MaskParams&
 // tested step by step); an empty one at directed distance d gives the cube of bricks from
 // it d-1 bricks ahead.  (Region-level cubes are not consulted: with directed brick cubes
 // they would shorten the walk by well under 1 % of lookups, less than their own cost.)
+// left: the ray's iterations left after the current one.  The box is cut to at most
+// left / 3 further steps per axis, so the ray leaves it by its last allowed iteration:
+// the step cap is then tested only when a box is left.
 // Returns T_LIVE, T_HIT (c is solid) or T_MISS (c is outside the alive ranges).
 __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, const MaskParams& P,
-                                         const int2* alive) {
+                                         const int2* alive, int left) {
     const Layout& L = P.L;
     const int2 ax = alive[r.oct * 3], ay = alive[r.oct * 3 + 1], az = alive[r.oct * 3 + 2];
     if ((unsigned)(cx - ax.x) >= (unsigned)ax.y || (unsigned)(cy - ay.x) >= (unsigned)ay.y ||
@@ -762,9 +768,11 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
               loz = max((bz - k) * four, P.cl[2]);
     const int hix = min((bx + k + 1) * four, P.cl[3]), hiy = min((by + k + 1) * four, P.cl[4]),
               hiz = min((bz + k + 1) * four, P.cl[5]);
-    set_axis(cx, r.sx, lox, hix, r.kx, r.ex);
-    set_axis(cy, r.sy, loy, hiy, r.ky, r.ey);
-    set_axis(cz, r.sz, loz, hiz, r.kz, r.ez);
+    const int kmax = (int)__umulhi((unsigned)max(left, 0), 0x55555556u);  // floor(left / 3)
+    set_axis(cx, r.sx, lox, hix, kmax, r.kx, r.ex);
+    set_axis(cy, r.sy, loy, hiy, kmax, r.ky, r.ey);
+    set_axis(cz, r.sz, loz, hiz, kmax, r.kz, r.ez);
+    r.lb = left - (r.kx + r.ky + r.kz);
     r.m = m;
     r.bi = (cx & 3) | ((cy & 3) << 2) | ((cz & 3) << 4);
     return ((m >> r.bi) & 1) ? T_HIT : T_LIVE;
@@ -801,12 +809,16 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
     // this loop.  (Doing the same for the box counters helped long empty boxes but cost
     // more on the 1080p frame, so those stay plain adds.)
     const int one = P.one, four = P.four, sixteen = P.sixteen;
-    // after the top-of-loop decrement r.left is negative on the last allowed iteration; with
-    // DF the float test decides instead, and r.left only counts (it cannot reach 0 first:
-    // caps are at most 2^24)
+    // The step cap.  An iteration lowers exactly one of kx, ky, kz, so lb + kx + ky + kz
+    // counts the iterations left after the current one without a counter of its own; it is
+    // negative on the last allowed iteration.  Every box is cut so that the ray leaves it
+    // by that iteration (enter_box), so the cap is tested only where a box is left.  With
+    // DF the float test decides instead, and the count only counts (it cannot reach 0
+    // first: caps are at most 2^24).
     constexpr int kCount = 1 << 30;
     const int left0 = DF ? kCount - 1 : n0 - 1;
-    r.left = left0;
+    r.lb = left0;
+    int left_end = left0;  // the count at the breaking iteration
     float travelled = 0.0f;
     const float lim = DF ? fminf((float)n, (float)maxSteps) : 0.0f;
     V3 start = o;
@@ -823,7 +835,6 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
         if (bx) r.kx -= 1;
         if (by) r.ky -= 1;
         if (bz) r.kz -= 1;
-        r.left -= 1;
         bool last = false;  // DF: no iteration follows this one
         if (DF) {
             travelled = fadd(travelled, 1.0f);
@@ -836,13 +847,15 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
             if (bz) r.bi = r.sz * sixteen + r.bi;
             hb = (r.m >> (r.bi & 63)) & 1;
         }
-        if (((r.kx | r.ky | r.kz | r.left) < 0) | hb | last) {
+        if (((r.kx | r.ky | r.kz) < 0) | hb | last) {
             const int a = bx ? 0 : (by ? 1 : 2);
             const bool out = (r.kx | r.ky | r.kz) < 0;
+            const int left = r.lb + r.kx + r.ky + r.kz;
+            left_end = left;
             if (out) {
                 refills++;
                 const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
-                const int t = enter_box(r, cx, cy, cz, P, alive);
+                const int t = enter_box(r, cx, cy, cz, P, alive, left);
                 if (t == T_HIT) { result = T_HIT; hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz; }
                 else if (t == T_MISS) result = T_MISS;
                 else result = T_LIVE;
@@ -851,7 +864,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
                 const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
                 hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz;
             } else {
-                result = T_MISS;  // the step cap: this was the last iteration
+                result = T_MISS;  // DF: the float cap, this was the last iteration
             }
             if (DF && result == T_HIT) {
                 const int32_t v = __ldg(P.words + hit_index);
@@ -866,6 +879,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
                     r.tz = fdiv(fsub((float)(ncz + (r.sz > 0)), start.z), d.z);
                     // no box yet: the first step from the new cell looks one up
                     r.kx = 0; r.ky = 0; r.kz = 0;
+                    r.lb = left;
                     r.ex = ncx + r.sx; r.ey = ncy + r.sy; r.ez = ncz + r.sz;
                     r.m = 0;
                     r.bi = 0;
@@ -883,13 +897,13 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
                 sgn = a == 0 ? r.sx : (a == 1 ? r.sy : r.sz);
                 break;
             }
-            if (DF ? last : r.left < 0) { result = T_MISS; break; }  // entered a box on the last iteration
+            if (DF ? last : left < 0) { result = T_MISS; break; }  // entered a box on the last iteration
         }
         if (bx) r.tx = fadd(r.tx, r.dx);
         if (by) r.ty = fadd(r.ty, r.dy);
         if (bz) r.tz = fadd(r.tz, r.dz);
     }
-    steps += left0 - r.left;  // r.left = left0 - 1 - (index of the breaking iteration)
+    steps += left0 - left_end;  // left_end = left0 - 1 - (index of the breaking iteration)
     start_out = start;
     return result;
 }
