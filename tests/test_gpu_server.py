@@ -137,6 +137,14 @@ def test_edits_are_ordered_within_a_world(cuda, worlds):
     vrt.lib().vrt_server_destroy(srv)
 
 
+def test_bad_configs_are_refused(cuda):
+    for cfg in [(1 << 30, 0, 4, 0, 0), (1 << 30, 3, 0, 0, 0), (0, 3, 4, 0, 0), (1 << 30, 3, 4, -1, 0),
+                (1 << 30, 3, 4, 0, 2)]:
+        h = C.c_void_p()
+        assert vrt.lib().vrt_server_create(C.byref(vrt.ServerConfig(*cfg)), C.byref(h)) == vrt.EINVAL, cfg
+        assert not h.value
+
+
 def test_budget_refuses_oversized_requests(cuda, worlds):
     _, b = worlds
     w = make_world(b.words, b.W, b.H)

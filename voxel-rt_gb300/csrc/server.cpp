@@ -355,8 +355,10 @@ extern "C" {
 int vrt_server_create(const vrt_server_config* cfg, vrt_server** out) {
     if (!cfg || !out) return set_error(VRT_EINVAL, "NULL argument");
     *out = nullptr;
-    if (cfg->slots < 1 || cfg->slots > 64 || cfg->max_batch < 1 || cfg->memory_budget_bytes == 0)
-        return set_error(VRT_EINVAL, "bad server config");
+    if (cfg->slots < 1 || cfg->slots > 64 || cfg->max_batch < 1 || cfg->memory_budget_bytes == 0 ||
+        cfg->max_wait_us < 0 || (cfg->image_memory != 0 && cfg->image_memory != 1))
+        return set_error(VRT_EINVAL, "bad server config (slots 1-64, max_batch >= 1, budget > 0, max_wait_us >= 0, "
+                                     "image_memory 0 or 1)");
     vrt_server* s = new vrt_server();
     s->cfg = *cfg;
     s->t0 = Clock::now();
