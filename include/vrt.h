@@ -247,7 +247,9 @@ int vrt_renderer_destroy(vrt_renderer* r);
 int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
                int32_t height, uint8_t* d_rgba, const vrt_debug_out* dbg, uint64_t* d_stats,
                const vrt_render_opts* opts, void* stream);
-/* vrt_render with the image in host memory; waits for the image before returning.
+/* vrt_render with the image in host memory (host_rgba: width*height*4 bytes, which the
+ * caller guarantees: the kernel may store to every one of them); waits for the image
+ * before returning.
  * - Page-locked host memory (vrt_host_alloc, cudaHostAlloc, cudaHostRegister; 4-byte
  *   aligned) with host_bands = 0: the kernel stores each pixel straight into it over the
  *   host link while it renders; nothing is staged or copied afterwards.
