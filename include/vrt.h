@@ -288,11 +288,17 @@ int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count,
  * cannot afford cudaMalloc's implicit device synchronisation.  It has no counterpart in
  * the reference.  It takes no renderer: its scratch (the view table, and the tile counter
  * of the persistent kernel) lives in a static device array of the library, about 46 KiB
- * per GPU, so it calls no cudaMalloc or cudaFree.  At most VRT_NOALLOC_MAX_VIEWS views per
- * call (more: VRT_ERANGE).  The first call on each device looks up the array's device
+ * per GPU, so it calls no cudaMalloc or cudaFree.  Limits:
+ *   - at most VRT_NOALLOC_MAX_VIEWS views per call (more: VRT_ERANGE);
+ *   - worlds without depth-field words only (VRT_ESTATE otherwise: the tile kernel's stop
+ *     masks for such worlds are allocated on first use).
+ * It checks and lays out views exactly as vrt_render_batch does.  The view table reaches
+ * the device inside kernel parameters, so nothing the call queues refers to the caller's
+ * views after it returns.  The first call on each device looks up the array's device
  * address (cudaGetSymbolAddress) and fills a 1 KiB table of the library, with that device
- * current; make that first call before any stream capture.  Every call shares the one array and resets its counter, so calls that overlap
- * on the GPU (other streams, other threads) race: order them on one stream. */
+ * current; make that first call before any stream capture.  Every call shares the one
+ * array and resets its counter, so calls that overlap on the GPU (other streams, other
+ * threads) race: order them on one stream. */
 #define VRT_NOALLOC_MAX_VIEWS 64
 int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, const vrt_render_opts* opts, void* stream);
 
@@ -342,7 +348,8 @@ typedef struct vrt_completion {
 
 int vrt_server_create(const vrt_server_config* cfg, vrt_server** out);
 int vrt_server_destroy(vrt_server* s);
-/* Register a resident world (not owned).  Returns its id in *id. */
+/* Register a resident world (not owned).  Returns its id in *id.  Thread-safe, also
+ * while another thread submits or polls. */
 int vrt_server_add_world(vrt_server* s, vrt_world* w, int32_t* id);
 /* Enqueue a request (thread-safe).  Edits of a world run after every earlier render of
  * that world and before every later one. */

@@ -2,13 +2,15 @@
 # Builds the reference's own C++ and its shader (read in place from the reference
 # checkout, never copied into this repository) into oracle/_ref/ for golden-vector
 # generation and oracle pinning.  Test infrastructure only; x86 or Arm, g++ only.
+# The checkout's src/ directory: $VRT_REFERENCE_SRC, else reference/src in the directory
+# that holds this repository.  Exits 3 (nothing built) when neither exists.
 #   oracle/_ref/librefworld.so   src/level.cpp + src/render.cpp + ref_world_stub.cpp
 #   oracle/_ref/librefshader.so  src/fshader.glsl via glsl_to_cpp.sed + refshader_harness.cpp
 # The reference's own build uses g++ -O2 (compile.bat:3); -ffp-contract=off keeps float
 # expressions unfused on CPUs with FMA.
 set -e
-REF=${VRT_REFERENCE_SRC:-/root/reference/src}
 HERE=$(cd "$(dirname "$0")" && pwd)
+REF=${VRT_REFERENCE_SRC:-$HERE/../../../reference/src}
 OUT=$HERE/../_ref
 if [ ! -f "$REF/fshader.glsl" ]; then echo "reference sources not found at $REF" >&2; exit 3; fi
 mkdir -p "$OUT"

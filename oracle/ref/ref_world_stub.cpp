@@ -114,6 +114,15 @@ void vrt_ref_light_pos(float rotation_deg, float* out3) {
     out3[0] = p.x; out3[1] = p.y; out3[2] = p.z;
 }
 
+// The reference's own lightUpdate (render.cpp:388-402) called `calls` times at frame rate
+// frame_rate, from lightRotation = start_deg: out4 = lightPos, then lightRotation.
+void vrt_ref_light_update(long long frame_rate, float start_deg, int calls, float* out4) {
+    fps = frame_rate;
+    lightRotation = start_deg;
+    for (int i = 0; i < calls; i++) lightUpdate();
+    out4[0] = lightPos.x; out4[1] = lightPos.y; out4[2] = lightPos.z; out4[3] = lightRotation;
+}
+
 // rotateMatrix of doMouseLook (controls.cpp:136-142) for camRotation (x, y).
 void vrt_ref_rotate_matrix(float rx, float ry, float* out16) {
     glm::mat4 rotX = glm::rotate(glm::mat4(1.0f), rx, glm::vec3(1, 0, 0));

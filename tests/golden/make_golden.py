@@ -6,7 +6,8 @@ reference's code, never from the oracle:
   - reference_world.json  sha256 and counts of initVoxels (level.cpp:82-138), of the
                           full fixDepthField pass (render.cpp:226-286), and of the world
                           after a sequence of removeSphere edits (level.cpp:30-56);
-                          placeLocalLight slot tables (render.cpp:375-385).
+                          placeLocalLight slot tables (render.cpp:375-385); lightPos
+                          and lightRotation after runs of lightUpdate (render.cpp:388-402).
   - shader_reference_scene.npz  the reference fragment shader (src/fshader.glsl compiled
                           as C++ against its vendored GLM) on a pixel subset of the
                           reference scene: 512x96x512 initVoxels world with its depth
@@ -49,6 +50,9 @@ EDITS = [((195, 40, 170), 7), ((3, 30, 200), 5), ((510, 35, 5), 8), ((100, 94, 1
          ((300, 36, 301), 0), ((60, 45, 75), 6)]
 
 # placeLocalLight calls (x, y, z, a); negative coordinates leave a slot free
+# lightUpdate runs: (fps, lightRotation at the start, calls).  The app starts at -45
+# degrees (main.cpp:36); 170 degrees crosses the fast night branch and wraps past 360.
+LIGHT_UPDATES = [(60, -45.0, 1), (60, -45.0, 600), (2, -45.0, 1000), (1, 170.0, 400), (144, 359.9, 50)]
 LIGHT_CALLS = [(10.0, 40.0, 10.0, 0.5), (-1.0, 5.0, 5.0, 0.5), (20.0, 41.5, 30.0, 0.7)] + \
               [(float(i), 45.0, float(2 * i), 0.5) for i in range(16)]
 
@@ -106,6 +110,17 @@ def main():
     lp = np.zeros(3, np.float32)
     L.vrt_ref_light_pos(C.c_float(-45.0), lp.ctypes.data)
     gold["light_pos_minus45"] = [float(v) for v in lp]
+    # the reference's own lightUpdate (float glm::rotate about +z), from the app's start
+    # (-45 degrees) at 60 fps, over many frames, and across the fast night branch and the wrap
+    L.vrt_ref_light_update.argtypes = [C.c_longlong, C.c_float, C.c_int, C.c_void_p]
+    seq = []
+    for (frame_rate, start, calls) in LIGHT_UPDATES:
+        out = np.zeros(4, np.float32)
+        L.vrt_ref_light_update(frame_rate, start, calls, out.ctypes.data)
+        seq.append({"fps": frame_rate, "start_deg": start, "calls": calls,
+                    "light_pos_bits": [int(v) for v in out[:3].view(np.uint32)],
+                    "rotation_bits": int(out[3:].view(np.uint32)[0])})
+    gold["light_update"] = seq
     rot = np.zeros(16, np.float32)
     L.vrt_ref_rotate_matrix(C.c_float(0.3), C.c_float(-1.1), rot.ctypes.data)
     gold["rotate_matrix_0.3_-1.1"] = [float(v) for v in rot]

@@ -8,7 +8,7 @@ import numpy as np
 import pytest
 
 import vrt
-from helpers import assert_same_frame
+from helpers import assert_same_frame, load_golden
 
 pytestmark = pytest.mark.gpu
 
@@ -18,7 +18,8 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 def test_dropin_main_renders_the_reference_scene(cuda, oracle, tmp_path):
     pkg = os.path.join(ROOT, "voxel-rt_gb300")
     exe = str(tmp_path / "dropin_main")
-    subprocess.run(["g++", "-std=c++17", "-O2", "-I" + os.path.join(pkg, "dropin"),
+    # no contracted multiply-adds (the reference's x86 build has none; g++ on Arm fuses by default)
+    subprocess.run(["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-I" + os.path.join(pkg, "dropin"),
                     os.path.join(ROOT, "tests", "dropin_main.cpp"), os.path.join(pkg, "dropin", "render_dropin.cpp"),
                     "-L" + pkg, "-lvrt", "-Wl,-rpath," + pkg, "-o", exe], check=True)
     out = subprocess.run([exe, str(tmp_path)], capture_output=True, text=True, timeout=300)
@@ -30,6 +31,9 @@ def test_dropin_main_renders_the_reference_scene(cuda, oracle, tmp_path):
     oracle.fix_depth_field_box(world, W, H, (0, 0, 0, W, H, W))
     u = vrt.default_uniforms()
     u.camPos[:] = list(params[0:3])
+    # lightUpdate(60) once from -45 degrees: the reference's own lightPos, bit for bit
+    first = [c for c in load_golden("reference_world.json")["light_update"] if c["calls"] == 1 and c["fps"] == 60][0]
+    assert [int(v) for v in params[3:6].view(np.uint32)] == first["light_pos_bits"]
     u.lightPos[:] = list(params[3:6])
     u.aspectRatio = float(params[6])
     u.maxSteps = int(params[7])

@@ -27,23 +27,33 @@ def _views(cuda, world, cams):
     return imgs, stats, (vrt.View * len(vv))(*vv)
 
 
-def test_noalloc_batch_equals_batch_on_two_calls_in_a_row(cuda):
+@pytest.mark.parametrize("count", [1, 12, 40])
+@pytest.mark.parametrize("kernel", [vrt.KERNEL_AUTO, vrt.KERNEL_BITMASK])
+def test_noalloc_batch_equals_batch_on_two_calls_in_a_row(cuda, kernel, count):
+    """Both kernels a batch can run: the tile kernel (AUTO), whose views travel in the static
+    array or, for one view, in the launch itself; and the persistent kernel (BITMASK), whose
+    tile counter lives in the static array too and must be cleared by every call.  40 views
+    take two copies of the view table."""
     sc = scenes.full(2, W=128, H=64, width=64, height=64, max_steps=256)
     world = make_world(sc.words, sc.W, sc.H)
-    cams = [(u, max(8, w // 8), max(6, h // 8)) for (u, w, h) in scenes.batch_views(sc, 12, seed=5)]
+    cams = [(u, max(8, w // 8), max(6, h // 8)) for (u, w, h) in scenes.batch_views(sc, count, seed=5)]
     for (u, w, h) in cams:
         u.aspectRatio = w / h
     stream = cuda.cuda.current_stream().cuda_stream
+    opts = vrt.RenderOpts()
+    opts.kernel = kernel
+    if kernel == vrt.KERNEL_BITMASK:
+        opts.tile_w, opts.tile_h = 8, 4
 
     ref_imgs, ref_stats, ref_arr = _views(cuda, world, cams)
     r = vrt.Renderer()
-    vrt.check(vrt.lib().vrt_render_batch(r.handle, ref_arr, len(cams), None, stream))
+    vrt.check(vrt.lib().vrt_render_batch(r.handle, ref_arr, len(cams), C.byref(opts), stream))
     cuda.cuda.synchronize()
     ref = [i.cpu().numpy() for i in ref_imgs]
 
     for call in range(2):
         imgs, stats, arr = _views(cuda, world, cams)
-        vrt.check(vrt.lib().vrt_render_batch_noalloc(arr, len(cams), None, stream))
+        vrt.check(vrt.lib().vrt_render_batch_noalloc(arr, len(cams), C.byref(opts), stream))
         cuda.cuda.synchronize()
         for i, (a, b) in enumerate(zip(ref, imgs)):
             d = np.abs(a.astype(np.int32) - b.cpu().numpy().astype(np.int32))

@@ -1492,9 +1492,14 @@ int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* 
     return VRT_OK;
 }
 
+// Checks a batch's views and fills its view table hv (room for count entries, host
+// memory): every view renders the one world, has a 4-byte aligned image of a valid size
+// and valid uniforms, and may pick its own tile shape of the launch's thread count; the
+// views' tiles are laid end to end in the launch's tile space.  Every batch entry point
+// goes through here, so all of them check and lay out views alike.
 // allow_df: the launch follows depth-field jumps (the tile kernel, launched now rather
 // than replayed from a graph that would keep stale stop masks after an edit).
-static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, std::vector<ViewDev>& hv,
+static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, ViewDev* hv,
                        const vrt_world** world_out, int* total_out, bool allow_df) {
     if (!views || count < 1) return set_error(VRT_EINVAL, "empty batch");
     const vrt_world* w = views[0].world;
@@ -1502,7 +1507,6 @@ static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, st
     if (w->has_depth_field && !allow_df)
         return set_error(VRT_ESTATE, "the world holds depth-field words: render it with vrt_render or vrt_render_batch "
                                      "and the tile kernel");
-    hv.resize(count);
     int tiles = 0;
     for (int i = 0; i < count; i++) {
         const vrt_view& v = views[i];
@@ -1542,10 +1546,10 @@ static int batch_tuning(const vrt_render_opts* opts, Tuning* t, bool* tiles) {
     return tile_tuning(opts, t);
 }
 
-static int launch_batch(vrt_renderer* r, const vrt_world* w, const std::vector<ViewDev>& hv, int total,
+static int launch_batch(vrt_renderer* r, const vrt_world* w, const ViewDev* hv, int count, int total,
                         const Tuning& t, bool tiles, const ViewDev* d_views, unsigned* d_counter, cudaStream_t s) {
-    if (tiles) return launch_tiles(w, hv.data(), (int)hv.size(), total, d_views, t.tile_w * t.tile_h, s);
-    return launch_mask(r, w, hv.data(), (int)hv.size(), total, t, d_views, d_counter, s);
+    if (tiles) return launch_tiles(w, hv, count, total, d_views, t.tile_w * t.tile_h, s);
+    return launch_mask(r, w, hv, count, total, t, d_views, d_counter, s);
 }
 
 int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count, const vrt_render_opts* opts,
@@ -1555,10 +1559,10 @@ int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count, cons
     bool tiles = true;
     int st = batch_tuning(opts, &t, &tiles);
     if (st) return st;
-    std::vector<ViewDev> hv;
+    std::vector<ViewDev> hv((size_t)std::max(count, 1));
     const vrt_world* w = nullptr;
     int total = 0;
-    st = build_batch(views, count, t, hv, &w, &total, tiles);
+    st = build_batch(views, count, t, hv.data(), &w, &total, tiles);
     if (st) return st;
     if (count > 1) {
         st = ensure_views(r, count);
@@ -1566,7 +1570,7 @@ int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count, cons
         // pageable source: the copy is staged before the call returns, so hv may go
         VRT_CUDA(cudaMemcpyAsync(r->d_views, hv.data(), sizeof(ViewDev) * count, cudaMemcpyHostToDevice, S(stream)));
     }
-    return launch_batch(r, w, hv, total, t, tiles, r->d_views, r->d_counter, S(stream));
+    return launch_batch(r, w, hv.data(), count, total, t, tiles, r->d_views, r->d_counter, S(stream));
 }
 
 int vrt_batch_graph_create(vrt_renderer* r, const vrt_view* views, int32_t count, const vrt_render_opts* opts,
@@ -1577,10 +1581,10 @@ int vrt_batch_graph_create(vrt_renderer* r, const vrt_view* views, int32_t count
     bool tiles = true;
     int st = batch_tuning(opts, &t, &tiles);
     if (st) return st;
-    std::vector<ViewDev> hv;
+    std::vector<ViewDev> hv((size_t)std::max(count, 1));
     const vrt_world* w = nullptr;
     int total = 0;
-    st = build_batch(views, count, t, hv, &w, &total, false);
+    st = build_batch(views, count, t, hv.data(), &w, &total, false);
     if (st) return st;
     vrt_batch_graph* g = new vrt_batch_graph();
     cudaError_t e = cudaMalloc(&g->d_views, sizeof(ViewDev) * (size_t)count);
@@ -1598,7 +1602,7 @@ int vrt_batch_graph_create(vrt_renderer* r, const vrt_view* views, int32_t count
         vrt_batch_graph_destroy(g);
         return cuda_error(e, "cudaStreamBeginCapture");
     }
-    st = launch_batch(r, w, hv, total, t, tiles, g->d_views, g->d_counter, g->capture_stream);
+    st = launch_batch(r, w, hv.data(), count, total, t, tiles, g->d_views, g->d_counter, g->capture_stream);
     e = cudaStreamEndCapture(g->capture_stream, &g->graph);
     if (st || e != cudaSuccess) {
         vrt_batch_graph_destroy(g);
@@ -1695,47 +1699,55 @@ static int noalloc_scratch(void** out) {
     return VRT_OK;
 }
 
+// The view table reaches the scratch array inside the parameters of copy kernels, up to
+// kViewsPerCopy views a launch (a launch's parameters hold at most 32764 bytes): the
+// runtime copies a launch's parameters when it is queued, so nothing queued by a call
+// refers to the caller's host memory or to this file's stack after the call returns.
+constexpr int kViewsPerCopy = 32;
+struct ViewChunk {
+    ViewDev v[kViewsPerCopy];
+};
+static_assert(sizeof(ViewChunk) + 16 <= 32764, "a view chunk must fit in one launch's parameters");
+static_assert(sizeof(ViewDev) % 4 == 0, "views are copied as 32-bit words");
+
+__global__ void copy_views_kernel(ViewDev* __restrict__ dst, const __grid_constant__ ViewChunk c, int n) {
+    const uint32_t* src = reinterpret_cast<const uint32_t*>(c.v);
+    uint32_t* out = reinterpret_cast<uint32_t*>(dst);
+    const int words = n * (int)(sizeof(ViewDev) / 4);
+    for (int i = threadIdx.x; i < words; i += blockDim.x) out[i] = src[i];
+}
+
 extern "C" int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, const vrt_render_opts* opts,
                                         void* stream) {
     if (!views || count < 1) return set_error(VRT_EINVAL, "empty batch");
     if (count > kNoAllocMaxViews)
         return set_error(VRT_ERANGE, "%d views exceed the %d the static scratch holds; split the batch", count,
                          kNoAllocMaxViews);
-    const vrt_world* w = views[0].world;
-    if (!w) return set_error(VRT_EINVAL, "view 0 has no world");
-    if (w->has_depth_field) return set_error(VRT_ESTATE, "batched rendering needs a world without depth-field words");
     Tuning t;
     bool tile_kernel = true;  // as vrt_render_batch: the tile kernel unless the persistent one is asked for
     int st = batch_tuning(opts, &t, &tile_kernel);
     if (st) return st;
-    ViewDev hv[kNoAllocMaxViews];  // host copy of the view table, on the stack
+    // The view checks and tile layout of vrt_render_batch; worlds with depth-field words
+    // are refused (VRT_ESTATE): their stop masks are allocated on first use.
+    ViewDev hv[kNoAllocMaxViews];  // host view table, on the stack
+    const vrt_world* w = nullptr;
     int tiles = 0;
-    for (int i = 0; i < count; i++) {
-        const vrt_view& v = views[i];
-        if (v.world != w) return set_error(VRT_EINVAL, "view %d renders another world; one batch = one world", i);
-        if (!v.d_rgba || ((uintptr_t)v.d_rgba & 3) || v.width < 1 || v.height < 1 || v.width > 32768 ||
-            v.height > 32768)
-            return set_error(VRT_EINVAL, "view %d: bad image (NULL, not 4-byte aligned, or out of range)", i);
-        st = check_uniforms(&v.uniforms);
-        if (st) return st;
-        Tuning tv = t;
-        if (tile_kernel && (v.tile_w > 0 || v.tile_h > 0)) {
-            if (v.tile_w < 1 || v.tile_h < 1 || v.tile_w * v.tile_h != t.tile_w * t.tile_h)
-                return set_error(VRT_EINVAL, "view %d: tile %dx%d does not have the launch's %d threads", i, v.tile_w,
-                                 v.tile_h, t.tile_w * t.tile_h);
-            tv.tile_w = v.tile_w;
-            tv.tile_h = v.tile_h;
-        }
-        fill_view(hv[i], v.uniforms, v.width, v.height, v.d_rgba, nullptr, v.d_stats, tv, tiles);
-        tiles += tiles_of(v.width, v.height, tv);
-    }
+    st = build_batch(views, count, t, hv, &w, &tiles, false);
+    if (st) return st;
     void* scratch = nullptr;
     st = noalloc_scratch(&scratch);
     if (st) return st;
     unsigned int* d_counter = reinterpret_cast<unsigned int*>(scratch);
     ViewDev* d_views = reinterpret_cast<ViewDev*>(static_cast<unsigned char*>(scratch) + kNoAllocCounterBytes);
-    if (count > 1)  // pageable source: the copy is staged before the call returns
-        VRT_CUDA(cudaMemcpyAsync(d_views, hv, sizeof(ViewDev) * count, cudaMemcpyHostToDevice, S(stream)));
+    if (count > 1) {  // a single view travels in the render launch's own parameters
+        ViewChunk chunk{};
+        for (int first = 0; first < count; first += kViewsPerCopy) {
+            const int n = std::min(kViewsPerCopy, count - first);
+            std::memcpy(chunk.v, hv + first, sizeof(ViewDev) * n);
+            copy_views_kernel<<<1, 256, 0, S(stream)>>>(d_views + first, chunk, n);
+            VRT_CUDA(cudaGetLastError());
+        }
+    }
     vrt_renderer shape;  // only its device and SM count are read
     VRT_CUDA(cudaGetDevice(&shape.device));
     if (tile_kernel) {

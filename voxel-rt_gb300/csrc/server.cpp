@@ -21,6 +21,7 @@
 #include <chrono>
 #include <cstring>
 #include <deque>
+#include <memory>
 #include <mutex>
 #include <thread>
 #include <vector>
@@ -92,9 +93,11 @@ struct ImagePool {
 struct vrt_server {
     vrt_server_config cfg;
     Clock::time_point t0;
-    std::mutex mu;  // guards queue
+    std::mutex mu;  // guards queue, done and the worlds list (not the entries it points to)
     std::deque<Queued> queue;
-    std::vector<WorldEntry> worlds;
+    // Entries are allocated one by one and never move: vrt_server_add_world may grow the
+    // list from any thread while the polling thread works on an entry it looked up.
+    std::vector<std::unique_ptr<WorldEntry>> worlds;
     std::vector<Slot> slots;
     ImagePool pool;
     uint64_t world_bytes = 0;
@@ -104,6 +107,13 @@ struct vrt_server {
 };
 
 using namespace vrt;
+
+// The entry of world `wid`: looked up under the lock, used without it (the entry's world
+// and event never change after vrt_server_add_world; has_edit is the polling thread's).
+static WorldEntry* world_entry(vrt_server* s, int wid) {
+    std::lock_guard<std::mutex> lk(s->mu);
+    return s->worlds[wid].get();
+}
 
 static void retire(vrt_server* s, Slot& sl) {
     double t = s->now();
@@ -148,7 +158,7 @@ static int wait_for_renders(vrt_server* s, int wid, cudaStream_t st, int self) {
 
 static int launch_edit(vrt_server* s, int si, const Queued& q) {
     Slot& sl = s->slots[si];
-    WorldEntry& we = s->worlds[q.req.world_id];
+    WorldEntry& we = *world_entry(s, q.req.world_id);
     int st = wait_for_renders(s, q.req.world_id, sl.stream, si);
     if (st) return st;
     if (we.has_edit) VRT_CUDA(cudaStreamWaitEvent(sl.stream, we.edit_event, 0));
@@ -213,7 +223,7 @@ static void release_images(vrt_server* s, Slot& sl) {
 static int launch_renders(vrt_server* s, int si, std::vector<Queued>& batch) {
     Slot& sl = s->slots[si];
     const int wid = batch[0].req.world_id;
-    WorldEntry& we = s->worlds[wid];
+    WorldEntry& we = *world_entry(s, wid);
     const bool on_device = s->cfg.image_memory == 1;
     uint64_t total = 0;
     for (auto& q : batch) total += q.bytes;
@@ -389,21 +399,23 @@ int vrt_server_destroy(vrt_server* s) {
         cudaFreeHost(sl.h_staging);
     }
     for (auto& we : s->worlds)
-        if (we.edit_event) cudaEventDestroy(we.edit_event);
+        if (we->edit_event) cudaEventDestroy(we->edit_event);
     delete s;
     return VRT_OK;
 }
 
 int vrt_server_add_world(vrt_server* s, vrt_world* w, int32_t* id) {
     if (!s || !w || !id) return set_error(VRT_EINVAL, "NULL argument");
-    if (s->world_bytes + w->device_bytes > s->cfg.memory_budget_bytes)
+    std::unique_ptr<WorldEntry> we(new WorldEntry());
+    we->w = w;
+    VRT_CUDA(cudaEventCreateWithFlags(&we->edit_event, cudaEventDisableTiming));
+    std::lock_guard<std::mutex> lk(s->mu);
+    if (s->world_bytes + w->device_bytes > s->cfg.memory_budget_bytes) {
+        cudaEventDestroy(we->edit_event);
         return set_error(VRT_EBUDGET, "world of %llu bytes exceeds the memory budget",
                          (unsigned long long)w->device_bytes);
-    WorldEntry we;
-    we.w = w;
-    VRT_CUDA(cudaEventCreateWithFlags(&we.edit_event, cudaEventDisableTiming));
-    std::lock_guard<std::mutex> lk(s->mu);
-    s->worlds.push_back(we);
+    }
+    s->worlds.push_back(std::move(we));
     s->world_bytes += w->device_bytes;
     *id = (int32_t)s->worlds.size() - 1;
     return VRT_OK;

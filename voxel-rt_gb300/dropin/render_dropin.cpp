@@ -149,16 +149,24 @@ void placeLocalLight(float x, float y, float z, float diffuse) {
         }
 }
 
-// lightUpdate (render.cpp:388-402): advance lightRotation and rotate startLightPos about +z.
+// lightUpdate (render.cpp:388-402): advance lightRotation and rotate startLightPos about +z,
+// in float and in the order of the reference's glm::rotate(mat4(1), radians(a), (0,0,1)) *
+// vec4(startLightPos, 1).  For the unit z axis that matrix has columns (c, s, 0, 0),
+// (-s, c, 0, 0), (0, 0, c + (1 - c), 0) and (0, 0, 0, 1); mat4 * vec4 sums
+// (m0*x + m1*y) + (m2*z + m3*w), whose zero terms drop out exactly.  Build this file
+// without contracted multiply-adds (-ffp-contract=off), as the reference's x86 build has
+// none, or x and y can differ in the last bit.
 void lightUpdate(float fps) {
     float increment = 0.3f / fps;
     if (lightRotation >= 360.0f) lightRotation = 0.0f;
     else if (lightRotation >= 180.0f && lightRotation < 270.0f) increment *= 8.0f;
     lightRotation += increment;
-    const double a = (double)lightRotation * 3.14159265358979323846 / 180.0;
-    const double c = std::cos(a), s = std::sin(a);
-    lightPos = vec3{(float)(c * startLightPos.x - s * startLightPos.y), (float)(s * startLightPos.x + c * startLightPos.y),
-                    startLightPos.z};
+    const float a = lightRotation * 0.01745329251994329576923690768489f;  // glm::radians
+    const float c = std::cos(a), s = std::sin(a);
+    const float czz = c + (1.0f - c);  // Rotate[2][2] = c + (1 - c) * axis.z * axis.z
+    const float ns = 0.0f - s;         // Rotate[1][0] = (1 - c) * axis.y * axis.x - s * axis.z
+    lightPos = vec3{c * startLightPos.x + ns * startLightPos.y, s * startLightPos.x + c * startLightPos.y,
+                    czz * startLightPos.z};
 }
 
 void updateUniforms() {
