@@ -10,10 +10,12 @@ with CUDA events on the launching stream.
   e2e        the same through vrt_render_to_host: uniforms in, RGBA8 image out to
              pinned host memory every step (the kernel stores the pixels into it over the
              host link), wall clock
-  roofline   effective bytes B = 4*steps + 4*primary hits + 4*pixels per frame (one
-             4-byte voxel word per DDA step in the reference shader) / kernel time,
-             against the measured HBM copy bandwidth; l2 fields against a measured L2
-             read bandwidth
+  roofline   instruction issue, the render kernel's bound: warp instructions per frame
+             (ncu, profiles/counters.json, captured on the same kernel sources) / frame
+             time, against 4 issue slots per SM per cycle at the sampled SM clock; beside
+             it the effective bandwidth (B = 4*steps + 4*primary hits + 4*pixels: one
+             4-byte voxel word per DDA step of the reference shader) and the physical
+             DRAM / L2 traffic ncu measured, against the measured HBM copy bandwidth
   batched    64 cameras of uneven size in one CUDA-graph-captured persistent launch vs
              one launch per camera
   served     Poisson stream over 4 resident worlds: p50/p99 latency and Mrays/s per rate
@@ -154,10 +156,25 @@ def cpu_baseline(scene, target_s: float, threads: int):
             "sample": f"{what}: {rays} rays in {dt:.2f} s", "seconds": dt / reps}
 
 
+def workload_config(sc, world_size: int) -> dict:
+    """The config object of both arms: what the workload is, nothing about who ran it."""
+    return {"workload": sc.workload, "world": f"{sc.W}x{sc.H}x{sc.W}", "image": f"{sc.width}x{sc.height}",
+            "max_steps": int(sc.uniforms.maxSteps),
+            "local_lights": sum(1 for i in range(16) if sc.uniforms.localLights[i][0] >= 0),
+            "seed": getattr(sc, "seed", None), "l2": "GPU arm: flushed before every timed frame (256 MiB write)",
+            "parallelism": f"replicas x{world_size}"}
+
+
 def run_reference(args):
     rank, world_size, _ = rank_info()
     if rank != 0:
         return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import vrt_oracle
+    import vrt
+    # the scene's host-only helpers from the oracle library's build: libvrt.so (the CUDA
+    # library) is never loaded by this arm
+    vrt.use_host_library(vrt_oracle.library_path(fast=True))
     import scenes
     threads = os.cpu_count() or 1
     sc = scenes.full(2, threads=threads)
@@ -172,7 +189,7 @@ def run_reference(args):
         "impl": "reference", "metric": METRIC, "value": val, "unit": UNIT, "n_gpus": world_size,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded terrain)",
-        "config": {"workload": sc.workload, "sample": steps[-1]["sample"]},
+        "config": workload_config(sc, world_size),
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": threads, "kind": "port", "cpu": steps[-1]["cpu"],
                          "sample": steps[-1]["sample"]},
         "e2e": {"value": val, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
@@ -183,14 +200,61 @@ def run_reference(args):
     return 0
 
 
-def load_traffic(kernel: str, workload: str):
-    p = os.path.join(ROOT, "profiles", "traffic.json")
+COUNTER_SOURCES = [os.path.join("voxel-rt_gb300", "csrc", n) for n in ("render.cu", "shade_common.cuh")]
+
+
+def kernel_source_hash() -> str:
+    """sha256 (16 hex digits) of the render kernels' sources, to match ncu counters to a build."""
+    import hashlib
+    h = hashlib.sha256()
+    for rel in COUNTER_SOURCES:
+        with open(os.path.join(ROOT, rel), "rb") as f:
+            h.update(f.read())
+    return h.hexdigest()[:16]
+
+
+def load_counters(kernel: str, workload: str):
+    """ncu counters of one launch of kernel on workload (profiles/counters.json): warp
+    instructions, DRAM and L2 bytes.  Returns (entry or None, fresh), fresh when they were
+    captured on the current kernel sources."""
+    p = os.path.join(ROOT, "profiles", "counters.json")
     if not os.path.exists(p):
-        return None
+        return None, False
     with open(p) as f:
         d = json.load(f)
-    e = d.get(kernel, {})
-    return e.get("bytes_per_launch") if e.get("workload") == workload else None
+    e = d.get(f"{kernel}:{workload}")
+    return e, bool(e) and e.get("source_sha16") == kernel_source_hash()
+
+
+def roofline_of(kname, workload, ms, clk, hbm_peak, peak_src, algo_bytes, sms):
+    """The render kernels are bound by instruction issue (integer/logic pipe), not by memory:
+    achieved = warp instructions per launch (ncu, profiles/counters.json) / the launch's
+    CUDA-event time; peak = 4 warp schedulers x one issue per cycle x SMs x the median SM
+    clock sampled during the timed frames.  Beside it: the effective bandwidth (the bytes
+    the reference shader would read: 4 B per DDA iteration + hit colour + pixel) and the
+    physical DRAM and L2 traffic ncu measured, against the measured HBM copy peak."""
+    t = ms * 1e-3
+    cnt, fresh = load_counters(kname, workload)
+    mhz = clk.get("sm_mhz") or clk.get("sm_max_mhz") or 2070.0
+    r = {"bound": "issue", "kernel": kname, "unit": "G warp-instructions/s", "achieved": None,
+         "peak": sms * 4 * mhz * 1e6 / 1e9, "frac": None, "traffic": None,
+         "sms": sms, "sm_mhz": mhz, "peak_source": "4 issue slots per SM per cycle at the sampled SM clock",
+         "effective_bytes_per_launch": algo_bytes, "effective_gbs": algo_bytes / t / 1e9}
+    if cnt:
+        r["counters"] = {"source": cnt.get("source"), "fresh": fresh, "captured_on": cnt.get("source_sha16")}
+    if cnt and fresh:
+        inst = cnt["warp_inst_per_launch"]
+        dram = cnt["dram_bytes_per_launch"]
+        r.update(achieved=inst / t / 1e9, traffic=dram, warp_inst_per_launch=inst)
+        r["frac"] = r["achieved"] / r["peak"]
+        r["physical"] = {"dram_bytes_per_launch": dram, "l2_bytes_per_launch": cnt.get("l2_bytes_per_launch"),
+                         "dram_gbs": dram / t / 1e9, "hbm_peak_gbs": hbm_peak, "hbm_peak_source": peak_src,
+                         "dram_frac_of_hbm": dram / t / 1e9 / hbm_peak}
+        if cnt.get("l2_bytes_per_launch"):
+            r["physical"]["l2_gbs"] = cnt["l2_bytes_per_launch"] / t / 1e9
+    else:
+        r["note"] = "no ncu counters captured on these kernel sources: frac not computed"
+    return r
 
 
 def main():
@@ -311,39 +375,25 @@ def main():
            "path": "vrt_render_to_host into page-locked host memory: the kernel's pixel stores cross the host "
                    "link as it renders (no staging copy); uniforms go in as kernel parameters"}
 
-    peak, peak_src = measured_peaks()
+    hbm_peak, peak_src = measured_peaks()
     algo_bytes = 4 * steps + 4 * hits + 4 * pixels
-    achieved = algo_bytes / (ms * 1e-3) / 1e9
     kauto = "word" if world.info().has_depth_field else "pixel"
     kname = {"pixel": "render_tiles_kernel", "mask": "render_mask_kernel", "word": "render_word_kernel"}[
         kauto if args.kernel == "auto" else args.kernel]
-    roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s", "frac": achieved / peak,
-                "traffic": load_traffic(kname, args.workload), "peak_source": peak_src,
-                "algorithmic_bytes_per_launch": algo_bytes, "kernel": kname,
-                "note": "effective bytes: one 4-byte word per DDA iteration of the shader (S counted exactly on the "
-                        "device, equal to the oracle's) + the colour word per primary hit + the RGBA8 store; the mask "
-                        "kernels read far fewer physical bytes (traffic) and end rays that cannot hit early "
-                        "(config.dda_steps_performed)"}
+    roofline = roofline_of(kname, args.workload, ms, clk, hbm_peak, peak_src, algo_bytes,
+                           torch.cuda.get_device_properties(dev).multi_processor_count)
 
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world_size, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f32", "data": sc.data,
-        "config": {"workload": sc.workload, "rays_per_frame": rays, "dda_steps_per_frame": steps,
-                   "dda_steps_performed": steps_performed, "box_lookups": int(st_fast[4]),
-                   "primary_hits": hits, "pixels": pixels, "kernel": kname, "tile": args.tile,
-                   "refill_min": args.refill, "l2": "flushed before every timed frame (256 MiB write)",
-                   "parallelism": f"replicas x{world_size}"},
+        "config": workload_config(sc, world_size),
+        "frame": {"rays": rays, "dda_steps": steps, "dda_steps_performed": steps_performed,
+                  "box_lookups": int(st_fast[4]), "primary_hits": hits, "pixels": pixels, "kernel": kname,
+                  "tile": args.tile, "refill_min": args.refill},
         "clocks": clk, "gpu_launches": args.steps, "roofline": roofline, "e2e": e2e,
         "frame_ms_min": min(times), "frame_ms_max": max(times),
     }
-    if rank == 0:
-        try:
-            l2 = vrt.probe_l2_read_gbs(64 << 20, 100)
-            roofline["l2_read_gbs_measured"] = l2
-            roofline["l2_frac"] = achieved / l2
-        except Exception as e:  # measurement helper only
-            roofline["l2_read_gbs_measured"] = f"failed: {e}"
     if rank == 0 and world_size == 1 and not args.no_extras:
         line["batched"] = bench_batched(vrt, torch, scenes, sc, world, r, dev, stream)
         line["served"] = bench_served(vrt, torch, scenes, sc, world)

@@ -47,29 +47,37 @@ def _load(fast: bool = False) -> C.CDLL:
     return _libs[name]
 
 
+def library_path(fast: bool = False) -> str:
+    """The oracle library (built if missing); it also exports the host-only scene helpers
+    of include/vrt.h (vrt.use_host_library)."""
+    _load(fast)
+    return os.path.join(HERE, "libvrt_oracle_fast.so" if fast else "libvrt_oracle.so")
+
+
 def _ptr(a):
     return None if a is None else a.ctypes.data
 
 
 def render(words: np.ndarray, W: int, H: int, uniforms, width: int, height: int, rows=None, threads: int = 0,
-           fast: bool = False, outputs: bool = True):
+           fast: bool = False, outputs=True):
     """Render rows of a width x height frame.  rows: None (all), or (begin, end, stride).
+    outputs: True (every per-pixel output), False (totals only) or a tuple of names out of
+    rgba, hit, cast, occ, steps, primary_steps, shade.
     Returns a dict of full-image arrays (unwritten rows zero) and the totals
     (rays cast, DDA iterations, primary hits, pixels)."""
     L = _load(fast)
     rb, re_, rs = (0, height, 1) if rows is None else rows
-    n = width * height
-    out = {}
-    if outputs:
-        out = {
-            "rgba": np.zeros((height, width, 4), np.uint8),
-            "hit": np.zeros((height, width), np.int32),
-            "cast": np.zeros((height, width), np.uint32),
-            "occ": np.zeros((height, width), np.uint32),
-            "steps": np.zeros((height, width), np.int32),
-            "primary_steps": np.zeros((height, width), np.int32),
-            "shade": np.zeros((height, width, 3), np.float32),
-        }
+    shapes = {
+        "rgba": ((height, width, 4), np.uint8),
+        "hit": ((height, width), np.int32),
+        "cast": ((height, width), np.uint32),
+        "occ": ((height, width), np.uint32),
+        "steps": ((height, width), np.int32),
+        "primary_steps": ((height, width), np.int32),
+        "shade": ((height, width, 3), np.float32),
+    }
+    names = tuple(shapes) if outputs is True else (tuple(outputs) if outputs else ())
+    out = {k: np.zeros(*shapes[k]) for k in names}
     totals = np.zeros(4, np.uint64)
     g = out.get
     st = L.vrt_oracle_render(words.ctypes.data, W, H, C.addressof(uniforms), width, height, rb, re_, rs,

@@ -46,11 +46,18 @@ def fcolor_from_outputs(words, hit, shade, primary_steps=None, depth_view=False)
     return col
 
 
+DEBUG_OUTPUTS = ("hit", "cast", "occ", "steps", "primary_steps", "shade")
+# the side outputs that leave a launch inexact (no step counts asked for): the launch the
+# bench times, with its per-pixel results made visible
+INEXACT_OUTPUTS = ("hit", "cast", "occ", "shade")
+
+
 def gpu_render(world: vrt.World, u: vrt.Uniforms, width: int, height: int, kernel: int = vrt.KERNEL_AUTO,
                tile=None, refill_min: int = 0, renderer: vrt.Renderer | None = None, debug: bool = True,
-               exact_steps: int = 0):
+               exact_steps: int = 0, outputs=None):
     """Render through the C ABI; with debug=True every debug output is requested (which
-    makes step accounting exact), with debug=False only the image and the counters."""
+    makes step accounting exact), with debug=False only the image and the counters;
+    outputs (a subset of DEBUG_OUTPUTS) requests just those side outputs."""
     import torch
     dev = torch.device("cuda")
     n = width * height
@@ -62,8 +69,9 @@ def gpu_render(world: vrt.World, u: vrt.Uniforms, width: int, height: int, kerne
     psteps = torch.zeros(n, dtype=torch.int32, device=dev)
     shade = torch.zeros(n * 3, dtype=torch.float32, device=dev)
     stats = torch.zeros(vrt.STAT_COUNT, dtype=torch.int64, device=dev)
-    dbg = vrt.DebugOut(hit.data_ptr(), cast.data_ptr(), occ.data_ptr(), steps.data_ptr(), psteps.data_ptr(),
-                       shade.data_ptr()) if debug else None
+    want = set(DEBUG_OUTPUTS if outputs is None else outputs) if (debug or outputs is not None) else set()
+    ptr = {"hit": hit, "cast": cast, "occ": occ, "steps": steps, "primary_steps": psteps, "shade": shade}
+    dbg = vrt.DebugOut(*[ptr[k].data_ptr() if k in want else None for k in DEBUG_OUTPUTS]) if want else None
     opts = vrt.RenderOpts()
     opts.kernel = kernel
     opts.exact_steps = exact_steps
@@ -86,17 +94,19 @@ def gpu_render(world: vrt.World, u: vrt.Uniforms, width: int, height: int, kerne
     }
 
 
-def assert_same_frame(o: dict, g: dict, rows=None):
+def assert_same_frame(o: dict, g: dict, rows=None, outputs=DEBUG_OUTPUTS):
     """Oracle vs GPU: hit index, cast/occlusion bits and step counts bit-exact; light
-    multipliers bit-exact; RGBA8 within RGB_TOL (and in practice equal)."""
+    multipliers bit-exact; RGBA8 within RGB_TOL (and in practice equal).  outputs names
+    the side outputs the GPU render was asked for (the image is always compared)."""
     sel = slice(None) if rows is None else rows
-    for key in ("hit", "cast", "occ", "steps", "primary_steps"):
+    for key in [k for k in ("hit", "cast", "occ", "steps", "primary_steps") if k in outputs]:
         a, b = np.asarray(o[key])[sel], np.asarray(g[key])[sel]
         bad = np.argwhere(a != b)
         assert bad.size == 0, f"{key}: {len(bad)} mismatches, first at {bad[:3].tolist()}: {a[tuple(bad[0])]} vs {b[tuple(bad[0])]}"
-    a = np.asarray(o["shade"])[sel].view(np.uint32)
-    b = np.asarray(g["shade"])[sel].view(np.uint32)
-    assert np.array_equal(a, b), f"shade: {(a != b).any(-1).sum()} pixels differ"
+    if "shade" in outputs:
+        a = np.asarray(o["shade"])[sel].view(np.uint32)
+        b = np.asarray(g["shade"])[sel].view(np.uint32)
+        assert np.array_equal(a, b), f"shade: {(a != b).any(-1).sum()} pixels differ"
     da = np.abs(np.asarray(o["rgba"])[sel].astype(np.int32) - np.asarray(g["rgba"])[sel].astype(np.int32))
     assert da.max(initial=0) <= RGB_TOL, f"rgba differs by {da.max()}"
     assert np.array_equal(np.asarray(o["rgba"])[sel], np.asarray(g["rgba"])[sel])

@@ -1,8 +1,11 @@
 """Host-side logic that needs no GPU: the occupancy-layout model used by the GPU tests,
 the uniform helpers of the C ABI, and the seeded scene builders."""
 import math
+import os
 
 import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 
 from helpers import expected_distances, expected_distances_brute, expected_masks, expected_masks_loops
 
@@ -66,3 +69,38 @@ def test_scenes_are_deterministic(vrt_lib):
     assert all(lit)
     v = scenes.batch_views(f, 8, seed=3)
     assert len(v) == 8 and all(240 <= h <= 1080 for _, _, h in v)
+
+
+def test_scene_helpers_in_the_oracle_library_match_libvrt(vrt_lib, oracle):
+    """The CPU baseline builds its scenes through the oracle library's copy of the host-only
+    helpers (without loading libvrt.so): the same terrain words, uniforms and matrices."""
+    import ctypes as C
+    import subprocess
+    import sys
+    vrt = vrt_lib
+    L = C.CDLL(oracle.library_path(fast=True))
+    for name in vrt.HOST_FUNCTIONS:
+        getattr(L, name).restype, getattr(L, name).argtypes = vrt.SIGNATURES[name]
+    a = np.empty(96 * 48 * 96, np.int32)
+    b = np.empty_like(a)
+    assert L.vrt_terrain_generate(a.ctypes.data, 96, 48, 77, 3) == 0
+    assert vrt.lib().vrt_terrain_generate(b.ctypes.data, 96, 48, 77, 2) == 0
+    assert np.array_equal(a, b)
+    assert L.vrt_terrain_height(512, 9, 100, 300) == vrt.lib().vrt_terrain_height(512, 9, 100, 300)
+    m1, m2 = (C.c_float * 16)(), (C.c_float * 16)()
+    L.vrt_rotate_matrix(0.4, -2.0, m1)
+    vrt.lib().vrt_rotate_matrix(0.4, -2.0, m2)
+    assert bytes(m1) == bytes(m2)
+    u1, u2 = vrt.Uniforms(), vrt.Uniforms()
+    L.vrt_uniforms_default(C.byref(u1))
+    vrt.lib().vrt_uniforms_default(C.byref(u2))
+    assert bytes(u1) == bytes(u2)
+    # a fresh process builds the 1080p scene through the oracle library alone
+    code = ("import sys; sys.path[:0] = [%r, %r]; import vrt, vrt_oracle, scenes; "
+            "vrt.use_host_library(vrt_oracle.library_path(fast=True)); sc = scenes.full(2, W=128, H=64); "
+            "import os; maps = open('/proc/self/maps').read(); print(scenes.words_hash(sc.words), "
+            "'libvrt.so' in maps)") % (os.path.join(ROOT, "voxel-rt_gb300"), os.path.join(ROOT, "oracle"))
+    out = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True, timeout=120, check=True)
+    h, loaded = out.stdout.split()
+    import scenes
+    assert h == scenes.words_hash(scenes.full(2, W=128, H=64).words) and loaded == "False"

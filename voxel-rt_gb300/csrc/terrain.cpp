@@ -14,7 +14,7 @@
 #include <thread>
 #include <vector>
 
-#include "vrt_internal.h"
+#include "vrt_host.h"
 
 namespace {
 

@@ -7,12 +7,11 @@
 #include <cstdio>
 #include <string>
 
-#include "../../include/vrt.h"
+#include "vrt_host.h"
 
 namespace vrt {
 
 // ---- error plumbing: every C entry point returns a status and records a message ----
-int set_error(int status, const char* fmt, ...);
 int cuda_error(cudaError_t e, const char* what);
 
 #define VRT_CUDA(call)                                       \

@@ -137,8 +137,8 @@ def full(seed: int = 2, W: int = 512, H: int = 256, width: int = 1920, height: i
     return Scene("full", W, H, seed, words, u, width, height, lights)
 
 
-def stress(seed: int = 5, threads: int = 0) -> Scene:
-    W, H = 2048, 256
+def stress(seed: int = 5, threads: int = 0, W: int = 2048) -> Scene:
+    H = 256
     rng = SplitMix64(seed)
     words = vrt.terrain_generate(W, H, seed, threads)
     lights = place_lights(rng, W, seed, 16)

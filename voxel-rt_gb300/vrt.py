@@ -225,30 +225,61 @@ def check(status: int) -> int:
     return status
 
 
+# The host-only entry points (csrc/host.cpp, csrc/terrain.cpp: uniform defaults, camera
+# matrix, light slots, seeded terrain).  They need no GPU; use_host_library() points them
+# at another build of the same sources, so a CPU-only process can build the seeded scenes
+# without loading libvrt.so.
+HOST_FUNCTIONS = ("vrt_last_error", "vrt_version", "vrt_uniforms_default", "vrt_init_local_lights",
+                  "vrt_place_local_light", "vrt_rotate_matrix", "vrt_terrain_generate", "vrt_terrain_height")
+_host_lib = None
+
+
+def use_host_library(path: str) -> None:
+    """Call the host-only entry points in the shared library at path (which exports them
+    with the signatures of include/vrt.h) instead of libvrt.so."""
+    global _host_lib
+    L = C.CDLL(path)
+    for name in HOST_FUNCTIONS:
+        fn = getattr(L, name)
+        fn.restype, fn.argtypes = SIGNATURES[name]
+    _host_lib = L
+
+
+def host_lib():
+    return _host_lib if _host_lib is not None else lib()
+
+
+def _hcheck(status: int) -> int:
+    if status < 0:
+        msg = host_lib().vrt_last_error()
+        raise VrtError(status, msg.decode() if msg else "")
+    return status
+
+
 # ---------------------------------------------------------------- uniforms (host only)
 
 def default_uniforms() -> Uniforms:
     """The reference's constants and start state (fshader.glsl:3-10, main.cpp:26-36)."""
     u = Uniforms()
-    check(lib().vrt_uniforms_default(C.byref(u)))
+    _hcheck(host_lib().vrt_uniforms_default(C.byref(u)))
     return u
 
 
 def rotate_matrix(pitch_x: float, yaw_y: float):
     """rotateMatrix = R_y(yaw) * R_x(pitch) (controls.cpp:136-142), column-major list."""
     m = (C.c_float * 16)()
-    check(lib().vrt_rotate_matrix(pitch_x, yaw_y, m))
+    _hcheck(host_lib().vrt_rotate_matrix(pitch_x, yaw_y, m))
     return list(m)
 
 
 def place_local_light(u: Uniforms, x: float, y: float, z: float, a: float) -> int:
     """placeLocalLight (render.cpp:375-385): returns the slot used or -1 when all are taken."""
-    slot = check(lib().vrt_place_local_light(C.byref(u), x, y, z, a))
+    slot = _hcheck(host_lib().vrt_place_local_light(C.byref(u), x, y, z, a))
     return -1 if slot >= MAX_LOCAL_LIGHTS else slot
 
 
 def init_local_lights(u: Uniforms) -> None:
-    check(lib().vrt_init_local_lights(C.byref(u)))
+    _hcheck(host_lib().vrt_init_local_lights(C.byref(u)))
 
 
 def set_camera(u: Uniforms, pos, pitch_x: float, yaw_y: float, width: int, height: int,
@@ -412,12 +443,12 @@ def make_view(world: World, u: Uniforms, width: int, height: int, d_rgba: int, d
 def terrain_generate(width: int, height: int, seed: int, threads: int = 0):
     import numpy as np
     words = np.empty(width * height * width, dtype=np.int32)
-    check(lib().vrt_terrain_generate(words.ctypes.data, width, height, seed, threads))
+    _hcheck(host_lib().vrt_terrain_generate(words.ctypes.data, width, height, seed, threads))
     return words
 
 
 def terrain_height(width: int, seed: int, x: int, z: int) -> int:
-    return check(lib().vrt_terrain_height(width, seed, x, z))
+    return _hcheck(host_lib().vrt_terrain_height(width, seed, x, z))
 
 
 def probe_l2_read_gbs(nbytes: int = 64 << 20, iters: int = 50) -> float:
