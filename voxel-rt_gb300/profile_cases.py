@@ -20,6 +20,11 @@ commands in profiles/*.md name the case and the kernel (-k) they capture.
                  (stop_mask_kernel rebuilds the stop masks, then the render), 2 rounds
   probe          1 Mi voxel probes of the 1080p world (probe_kernel), 3 launches
   world_build    upload of the 1080p world (brick_mask, parent_mask, dir_pass, cheb_pass)
+  reference_build  the reference world on the device: initVoxels (init_reference_layers,
+                 init_reference_trees), then fixDepthField over the whole world
+  reference_frame  the reference app's first frame (its world with the depth field, camera
+                 (195,55,155), 800x600, 384 steps), rendered by the kernel AUTO picks (the
+                 word kernel), 2 launches
   all            every case above, one after the other
 
 Usage: python voxel-rt_gb300/profile_cases.py CASE
@@ -158,6 +163,19 @@ def case_world_build(torch):
     _frame_world()
     torch.cuda.synchronize()
     return "upload of the 512x256x512 world"
+
+
+def case_reference_build(torch):
+    _reference_world()
+    torch.cuda.synchronize()
+    return "reference world: initVoxels + fixDepthField (512x96x512)"
+
+
+def case_reference_frame(torch):
+    w = _reference_world()
+    u = scenes.reference_scene_uniforms()
+    _render(torch, w, u, 800, 600, 2)
+    return "reference world, 800x600, AUTO kernel: 2 frames"
 
 
 CASES = {name[5:]: fn for name, fn in globals().items() if name.startswith("case_")}
