@@ -272,14 +272,18 @@ typedef struct vrt_view {
     int32_t width, height;
     uint8_t* d_rgba;        /* width*height*4 device bytes */
     uint64_t* d_stats;      /* optional, as vrt_render     */
-    int32_t tile_w, tile_h; /* this view's ray tile in the tile kernel (0 = the launch's);
-                               tile_w*tile_h must equal the launch's tile size */
+    int32_t tile_w, tile_h; /* this view's ray tile (0 = the launch's): in the tile kernel
+                               tile_w*tile_h must equal the launch's tile size; the persistent
+                               kernel takes any tile of 1 to 1024 pixels */
+    int32_t refill_min;     /* persistent kernel: lanes parked before a warp working on this
+                               view's tiles runs its refill phase, 1-32 (0 = the launch's) */
 } vrt_view;
 
 /* Many cameras of one world, of uneven sizes, in one launch: the tile kernel over every
  * view's ray tiles (each view may pick its own tile shape of the launch's thread count),
- * or with VRT_KERNEL_BITMASK the persistent kernel, which hands tiles out from a counter
- * and needs a world without depth-field words. */
+ * or with VRT_KERNEL_BITMASK the persistent kernel, which hands tiles out from a counter,
+ * lets each view choose its tile and live-ray refill interval, and needs a world without
+ * depth-field words. */
 int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count,
                      const vrt_render_opts* opts, void* stream);
 

@@ -113,3 +113,32 @@ def test_per_view_tiles_and_autotuner(cuda, batch_setup):
     bad = [vrt.make_view(w, views[0][0], views[0][1], views[0][2], ptrs[0], 0, (8, 8))]
     with pytest.raises(vrt.VrtError):
         r.render_batch(bad, None)  # 64 threads in a 128-thread launch
+
+
+def test_persistent_kernel_per_view_tiles_and_refill(cuda, batch_setup):
+    """The persistent kernel takes a tile and a live-ray refill interval per view (any tile
+    of up to 1024 pixels): images and ray counts stay those of the tile kernel's batch."""
+    import autotune
+    sc, views = batch_setup
+    w = make_world(sc.words, sc.W, sc.H)
+    r = vrt.Renderer()
+    base, bstats = _batch(cuda, r, w, views)
+    plan = autotune.Plan(vrt.KERNEL_BITMASK, (8, 4), {"small": (16, 8), "medium": (32, 1), "large": (8, 8)}, 8,
+                         class_refill={"small": 4, "medium": 16, "large": 32})
+    imgs = [cuda.zeros(vw * vh * 4, dtype=cuda.uint8, device="cuda") for (_, vw, vh) in views]
+    stats = cuda.zeros((len(views), vrt.STAT_COUNT), dtype=cuda.int64, device="cuda")
+    vv = plan.views(w, views, [i.data_ptr() for i in imgs], [stats[i].data_ptr() for i in range(len(views))])
+    assert {v.refill_min for v in vv} >= {4, 16}
+    r.render_batch(vv, plan.opts(), cuda.cuda.current_stream().cuda_stream)
+    cuda.cuda.synchronize()
+    for a, b in zip(base, imgs):
+        assert np.array_equal(a, b.cpu().numpy())
+    assert np.array_equal(bstats[:, [0, 2, 3]], stats.cpu().numpy()[:, [0, 2, 3]])
+    bad = plan.views(w, views[:1], [imgs[0].data_ptr()])
+    bad[0].refill_min = 33
+    with pytest.raises(vrt.VrtError):
+        r.render_batch(bad, plan.opts())
+    bad[0].refill_min = 0
+    bad[0].tile_w, bad[0].tile_h = 64, 32  # 2048 pixels
+    with pytest.raises(vrt.VrtError):
+        r.render_batch(bad, plan.opts())

@@ -1499,7 +1499,7 @@ int vrt_render_to_host(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* 
 // goes through here, so all of them check and lay out views alike.
 // allow_df: the launch follows depth-field jumps (the tile kernel, launched now rather
 // than replayed from a graph that would keep stale stop masks after an edit).
-static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, ViewDev* hv,
+static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, bool tile_kernel, ViewDev* hv,
                        const vrt_world** world_out, int* total_out, bool allow_df) {
     if (!views || count < 1) return set_error(VRT_EINVAL, "empty batch");
     const vrt_world* w = views[0].world;
@@ -1516,14 +1516,18 @@ static int build_batch(const vrt_view* views, int32_t count, const Tuning& t, Vi
             return set_error(VRT_EINVAL, "view %d: bad image (NULL, not 4-byte aligned, or out of range)", i);
         int st = check_uniforms(&v.uniforms);
         if (st) return st;
-        Tuning tv = t;  // a view may choose its own tile shape of the launch's tile size
+        Tuning tv = t;  // a view may choose its own tile shape (the tile kernel: of the launch's tile size)
         if (v.tile_w > 0 || v.tile_h > 0) {
-            if (v.tile_w < 1 || v.tile_h < 1 || v.tile_w * v.tile_h != t.tile_w * t.tile_h)
-                return set_error(VRT_EINVAL, "view %d: tile %dx%d does not have the launch's %d threads", i, v.tile_w,
-                                 v.tile_h, t.tile_w * t.tile_h);
+            if (v.tile_w < 1 || v.tile_h < 1 ||
+                (tile_kernel ? v.tile_w * v.tile_h != t.tile_w * t.tile_h : v.tile_w * v.tile_h > 1024))
+                return set_error(VRT_EINVAL, "view %d: tile %dx%d %s", i, v.tile_w, v.tile_h,
+                                 tile_kernel ? "does not have the launch's thread count" : "exceeds 1024 pixels");
             tv.tile_w = v.tile_w;
             tv.tile_h = v.tile_h;
         }
+        if (v.refill_min < 0 || v.refill_min > 32)
+            return set_error(VRT_EINVAL, "view %d: refill_min %d outside 0-32", i, v.refill_min);
+        if (v.refill_min > 0) tv.refill_min = v.refill_min;
         fill_view(hv[i], v.uniforms, v.width, v.height, v.d_rgba, nullptr, v.d_stats, tv, tiles);
         tiles += tiles_of(v.width, v.height, tv);
     }
@@ -1562,7 +1566,7 @@ int vrt_render_batch(vrt_renderer* r, const vrt_view* views, int32_t count, cons
     std::vector<ViewDev> hv((size_t)std::max(count, 1));
     const vrt_world* w = nullptr;
     int total = 0;
-    st = build_batch(views, count, t, hv.data(), &w, &total, tiles);
+    st = build_batch(views, count, t, tiles, hv.data(), &w, &total, tiles);
     if (st) return st;
     if (count > 1) {
         st = ensure_views(r, count);
@@ -1584,7 +1588,7 @@ int vrt_batch_graph_create(vrt_renderer* r, const vrt_view* views, int32_t count
     std::vector<ViewDev> hv((size_t)std::max(count, 1));
     const vrt_world* w = nullptr;
     int total = 0;
-    st = build_batch(views, count, t, hv.data(), &w, &total, false);
+    st = build_batch(views, count, t, tiles, hv.data(), &w, &total, false);
     if (st) return st;
     vrt_batch_graph* g = new vrt_batch_graph();
     cudaError_t e = cudaMalloc(&g->d_views, sizeof(ViewDev) * (size_t)count);
@@ -1732,7 +1736,7 @@ extern "C" int vrt_render_batch_noalloc(const vrt_view* views, int32_t count, co
     ViewDev hv[kNoAllocMaxViews];  // host view table, on the stack
     const vrt_world* w = nullptr;
     int tiles = 0;
-    st = build_batch(views, count, t, hv, &w, &tiles, false);
+    st = build_batch(views, count, t, tile_kernel, hv, &w, &tiles, false);
     if (st) return st;
     void* scratch = nullptr;
     st = noalloc_scratch(&scratch);

@@ -370,6 +370,7 @@ struct DepthOff {
 };
 __constant__ DepthOff c_depth_offs[1536];  // 1413 offsets of the radius-7 sphere have d > -6
 __constant__ int c_depth_count;
+__device__ DepthOff g_depth_offs[1536];    // the same table, read by the lanes of a warp at once
 static std::once_flag g_depth_once;
 static int g_depth_count = 0;
 static std::vector<DepthOff> g_depth_table;
@@ -395,6 +396,7 @@ static int ensure_depth_table() {
     std::call_once(g_depth_once, build_depth_table);
     // constant memory is per device: upload each time (cheap, 8 KB) to stay correct on any device
     VRT_CUDA(cudaMemcpyToSymbol(c_depth_offs, g_depth_table.data(), g_depth_table.size() * sizeof(DepthOff)));
+    VRT_CUDA(cudaMemcpyToSymbol(g_depth_offs, g_depth_table.data(), g_depth_table.size() * sizeof(DepthOff)));
     VRT_CUDA(cudaMemcpyToSymbol(c_depth_count, &g_depth_count, sizeof(int)));
     return VRT_OK;
 }
@@ -429,6 +431,60 @@ __global__ void fix_depth_field_kernel(int32_t* words, Layout L, int x0, int y0,
         }
     }
     if (nearest < 0.0f) words[idx] = __float_as_int(nearest);
+}
+
+// fix_depth_field_kernel with one warp per voxel, for edit-sized boxes: one thread per
+// voxel leaves most SMs idle there while each thread walks the offset table in turn.  The
+// lanes test 32 consecutive table offsets at a time and a ballot picks the first solid
+// one in table order -- the offset the one-thread loop stops at -- so the words written
+// are the same.
+__global__ void fix_depth_field_warp_kernel(int32_t* words, Layout L, int x0, int y0, int z0, int nx, int ny,
+                                            int nz, int cx, int cy, int cz, int r2) {
+    const uint64_t t = ((uint64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;  // this warp's voxel
+    const int lane = threadIdx.x & 31;
+    if (t >= (uint64_t)nx * ny * nz) return;  // the returns before the ballot are warp-uniform
+    const int x = x0 + (int)(t % nx), y = y0 + (int)((t / nx) % ny), z = z0 + (int)(t / ((uint64_t)nx * ny));
+    if (x < 0 || y < 0 || z < 0 || x >= L.W || y >= L.H || z >= L.W) return;
+    if (r2 > 0) {
+        const int ox = x - cx, oy = y - cy, oz = z - cz;
+        if (ox * ox + oy * oy + oz * oz >= r2 * r2) return;
+    }
+    const uint64_t idx = (uint64_t)x + (uint64_t)L.W * y + (uint64_t)L.W * L.H * z;
+    if (words[idx] >= 0) return;
+    float nearest = -6.0f;  // -DEPTH_FIELD_RADIUS + 1
+    const int n = c_depth_count;
+    for (int base = 0; base < n; base += 32) {
+        const int i = base + lane;
+        bool solid = false;
+        if (i < n) {
+            const DepthOff o = g_depth_offs[i];
+            const int qx = x + o.x, qy = y + o.y, qz = z + o.z;
+            if (qx >= 0 && qy >= 0 && qz >= 0 && qx < L.W && qy < L.H && qz < L.W)
+                solid = words[(uint64_t)qx + (uint64_t)L.W * qy + (uint64_t)L.W * L.H * qz] >= 0;  // plain load
+        }
+        const unsigned hits = __ballot_sync(0xffffffffu, solid);
+        if (hits) {
+            const float d = g_depth_offs[base + __ffs(hits) - 1].dist;
+            nearest = d <= -2.0f ? d : 0.0f;
+            break;
+        }
+    }
+    if (lane == 0 && nearest < 0.0f) words[idx] = __float_as_int(nearest);
+}
+
+// Boxes of at most this many voxels take the warp-per-voxel kernel (the edit of a
+// radius-1024 sphere would otherwise launch 2^38 threads).
+constexpr uint64_t kWarpPerVoxelMax = 1ull << 22;
+
+static void launch_fix_depth_field(vrt_world* w, int x0, int y0, int z0, int nx, int ny, int nz, int cx, int cy, int cz,
+                                   int r2, cudaStream_t s) {
+    const uint64_t n = (uint64_t)nx * ny * nz;
+    if (n <= kWarpPerVoxelMax)
+        fix_depth_field_warp_kernel<<<blocks_for(n * 32, 256), 256, 0, s>>>(w->d_words, w->L, x0, y0, z0, nx, ny, nz,
+                                                                            cx, cy, cz, r2);
+    else
+        fix_depth_field_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_words, w->L, x0, y0, z0, nx, ny, nz, cx, cy,
+                                                                  cz, r2);
 }
 
 __global__ void probe_kernel(const int32_t* __restrict__ words, Layout L, const int32_t* __restrict__ xyz, int n,
@@ -744,9 +800,7 @@ int vrt_fix_depth_field_box(vrt_world* w, int32_t x0, int32_t y0, int32_t z0, in
     if (x0 >= x1 || y0 >= y1 || z0 >= z1) return VRT_OK;
     int st = ensure_depth_table();
     if (st) return st;
-    uint64_t n = (uint64_t)(x1 - x0) * (y1 - y0) * (z1 - z0);
-    fix_depth_field_kernel<<<blocks_for(n, 256), 256, 0, S(stream)>>>(w->d_words, w->L, x0, y0, z0, x1 - x0,
-                                                                      y1 - y0, z1 - z0, 0, 0, 0, 0);
+    launch_fix_depth_field(w, x0, y0, z0, x1 - x0, y1 - y0, z1 - z0, 0, 0, 0, 0, S(stream));
     VRT_CUDA(cudaGetLastError());
     w->has_depth_field = 1;
     return refresh_masks_box(w, x0, y0, z0, x1, y1, z1, S(stream));
@@ -765,10 +819,8 @@ int vrt_remove_sphere(vrt_world* w, int32_t cx, int32_t cy, int32_t cz, int32_t 
     if (refresh_depth_field && r2 > 0) {
         int st = ensure_depth_table();
         if (st) return st;
-        int n = 2 * r2;
-        uint64_t cnt = (uint64_t)n * n * n;
-        fix_depth_field_kernel<<<blocks_for(cnt, 256), 256, 0, S(stream)>>>(w->d_words, w->L, cx - r2, cy - r2,
-                                                                            cz - r2, n, n, n, cx, cy, cz, r2);
+        const int n = 2 * r2;
+        launch_fix_depth_field(w, cx - r2, cy - r2, cz - r2, n, n, n, cx, cy, cz, r2, S(stream));
         VRT_CUDA(cudaGetLastError());
         w->has_depth_field = 1;
     }

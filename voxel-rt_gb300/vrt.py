@@ -105,6 +105,7 @@ class View(C.Structure):
         ("d_stats", C.c_void_p),
         ("tile_w", C.c_int32),
         ("tile_h", C.c_int32),
+        ("refill_min", C.c_int32),
     ]
 
 
@@ -428,7 +429,7 @@ class Renderer:
 
 
 def make_view(world: World, u: Uniforms, width: int, height: int, d_rgba: int, d_stats: int = 0,
-              tile=None) -> View:
+              tile=None, refill_min: int = 0) -> View:
     v = View()
     v.world = world.handle
     v.uniforms = u
@@ -437,6 +438,7 @@ def make_view(world: World, u: Uniforms, width: int, height: int, d_rgba: int, d
     v.d_stats = d_stats
     if tile:
         v.tile_w, v.tile_h = tile
+    v.refill_min = refill_min
     return v
 
 
