@@ -123,12 +123,12 @@ def test_persistent_kernel_per_view_tiles_and_refill(cuda, batch_setup):
     w = make_world(sc.words, sc.W, sc.H)
     r = vrt.Renderer()
     base, bstats = _batch(cuda, r, w, views)
-    plan = autotune.Plan(vrt.KERNEL_BITMASK, (8, 4), {"small": (16, 8), "medium": (32, 1), "large": (8, 8)}, 8,
-                         class_refill={"small": 4, "medium": 16, "large": 32})
+    plan = autotune.Plan(vrt.KERNEL_BITMASK, (8, 4), {}, 8)
     imgs = [cuda.zeros(vw * vh * 4, dtype=cuda.uint8, device="cuda") for (_, vw, vh) in views]
     stats = cuda.zeros((len(views), vrt.STAT_COUNT), dtype=cuda.int64, device="cuda")
-    vv = plan.views(w, views, [i.data_ptr() for i in imgs], [stats[i].data_ptr() for i in range(len(views))])
-    assert {v.refill_min for v in vv} >= {4, 16}
+    shapes = [((16, 8), 4), ((32, 1), 16), ((8, 8), 32), ((5, 3), 1), ((64, 16), 8)]
+    vv = [vrt.make_view(w, u, vw, vh, imgs[i].data_ptr(), stats[i].data_ptr(), *shapes[i % len(shapes)])
+          for i, (u, vw, vh) in enumerate(views)]
     r.render_batch(vv, plan.opts(), cuda.cuda.current_stream().cuda_stream)
     cuda.cuda.synchronize()
     for a, b in zip(base, imgs):

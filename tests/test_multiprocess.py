@@ -48,3 +48,24 @@ def test_two_rank_replicas():
     assert cams == list(range(64))
     assert t0 == t1 == 2.0  # the slowest rank's time on every rank
     assert rate0 == rate1 == 64 / 2.0
+
+
+def test_bench_reference_arm_under_torchrun_two_ranks(oracle):
+    """bench.py --impl reference launched as the driver launches N > 1 (torchrun, two
+    ranks): rank 0 alone times the CPU restatement and prints one JSON line, with the
+    workload config of the GPU arm; the other rank exits 0 without work."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2", "--master-addr",
+           "127.0.0.1", "--master-port", str(_free_port()), os.path.join(root, "bench.py"), "--impl", "reference",
+           "--gpus", "2", "--steps", "1", "--warmup", "0", "--cpu-seconds", "0.4"]
+    out = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=root)
+    assert out.returncode == 0, out.stderr[-2000:]
+    lines = [json.loads(line) for line in out.stdout.splitlines() if line.startswith("{")]
+    assert len(lines) == 1
+    d = lines[0]
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
+    assert d["config"]["world"] == "512x256x512" and d["config"]["parallelism"] == "replicas x2"
+    assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"

@@ -778,6 +778,48 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
     return ((m >> r.bi) & 1) ? T_HIT : T_LIVE;
 }
 
+// enter_box for worlds without depth-field words, where a ray only ever moves forward
+// along each axis.  cast_box checks the ray's first cell against the near side of the
+// world (and of the clip box along an axis the ray does not move along) once; every later
+// cell lies on the inner side of those bounds, so here only the far side of the clip box
+// [cl[0], cl[3]) x [cl[1], cl[4]) x [cl[2], cl[5]) can end the ray:
+//   kclip = s > 0 ? hi - 1 - c : c - lo     (steps before the far clip face; INT_MAX if s == 0)
+// kclip < 0 along some axis: the cell is beyond that face (outside the world, or beyond
+// the solid box in the direction of travel), which ends the ray as a miss.  Otherwise the
+// box along each axis is the rest of the brick plus 4 cells per further brick of an empty
+// cube, cut at the clip face and the step cap:
+//   k = min((s > 0 ? 3 - (c & 3) : c & 3) + 4 kk, kclip, kmax)
+// which is enter_box's box without its near-side bounds.  (An axis the ray does not move
+// along steps only when its intersect is -inf or NaN; its cell stays put and its k only
+// decides how often the box is looked up again.)  This is about 20 instructions shorter
+// than enter_box, and the box lookup runs in nearly every warp iteration.
+__device__ __forceinline__ int clip_far(int s, int c, int lo, int hi) {
+    return s > 0 ? hi - 1 - c : (s < 0 ? c - lo : INT_MAX);
+}
+__device__ __forceinline__ int enter_box_lean(BoxRay& r, int cx, int cy, int cz, const MaskParams& P, int left) {
+    const Layout& L = P.L;
+    const int kcx = clip_far(r.sx, cx, P.cl[0], P.cl[3]);
+    const int kcy = clip_far(r.sy, cy, P.cl[1], P.cl[4]);
+    const int kcz = clip_far(r.sz, cz, P.cl[2], P.cl[5]);
+    if ((kcx | kcy | kcz) < 0) return T_MISS;
+    const int bx = cx >> 2, by = cy >> 2, bz = cz >> 2;
+    const uint32_t bidx = (uint32_t)bx + (uint32_t)L.BWp * ((uint32_t)by + (uint32_t)L.BHp * (uint32_t)bz);
+    const uint64_t m = __ldg(P.bricks + bidx);
+    const int db = __ldg(P.bdir + (bidx * 8u + r.oct));
+    const int kk4 = m ? 0 : (max(db, 1) - 1) * P.four;
+    const int kmax = (int)__umulhi((unsigned)max(left, 0), 0x55555556u);  // floor(left / 3)
+    r.kx = min(min((((r.sx > 0) ? ~cx : cx) & 3) + kk4, kcx), kmax);
+    r.ky = min(min((((r.sy > 0) ? ~cy : cy) & 3) + kk4, kcy), kmax);
+    r.kz = min(min((((r.sz > 0) ? ~cz : cz) & 3) + kk4, kcz), kmax);
+    r.ex = r.sx * (r.kx + 1) + cx;
+    r.ey = r.sy * (r.ky + 1) + cy;
+    r.ez = r.sz * (r.kz + 1) + cz;
+    r.lb = left - (r.kx + r.ky + r.kz);
+    r.m = m;
+    r.bi = (cx & 3) | ((cy & 3) << 2) | ((cz & 3) << 4);
+    return ((m >> r.bi) & 1) ? T_HIT : T_LIVE;
+}
+
 // castRay (fshader.glsl:59-129) over the occupancy hierarchy.  Every iteration makes the
 // shader's comparison and its one intersect add, in the shader's order; memory is read
 // only when the ray leaves its known box.  On a hit, cd / axis / sgn / cell describe the
@@ -822,6 +864,24 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
     float travelled = 0.0f;
     const float lim = DF ? fminf((float)n, (float)maxSteps) : 0.0f;
     V3 start = o;
+    if (!DF) {
+        // The first cell (the start cell stepped along the first iteration's axis) must lie on
+        // the inner side of the near world bound along every axis the ray moves along, and
+        // within the clip box along an axis it does not move along; the ray then stays there
+        // (lookups test only the far side).  Otherwise it ends at its first iteration, as the
+        // shader's getVoxelIndex == -1 (or, for inexact launches, no solid voxel ahead) does.
+        const bool fx = (s.tx < s.ty) & (s.tx < s.tz);
+        const bool fy = (s.ty < s.tx) & (s.ty < s.tz);
+        const int c1x = s.cx + (fx ? s.sx : 0), c1y = s.cy + (fy ? s.sy : 0), c1z = s.cz + ((fx | fy) ? 0 : s.sz);
+        const bool dead =
+            (s.sx > 0 ? c1x < 0 : (s.sx < 0 ? c1x >= P.L.W : (c1x < P.cl[0] || c1x >= P.cl[3]))) ||
+            (s.sy > 0 ? c1y < 0 : (s.sy < 0 ? c1y >= P.L.H : (c1y < P.cl[1] || c1y >= P.cl[4]))) ||
+            (s.sz > 0 ? c1z < 0 : (s.sz < 0 ? c1z >= P.L.W : (c1z < P.cl[2] || c1z >= P.cl[5])));
+        if (dead) {
+            steps += 1;
+            return T_MISS;
+        }
+    }
     // no box yet: the first step along any axis (even one with s == 0) triggers a lookup
     r.kx = 0; r.ky = 0; r.kz = 0;
     r.ex = s.cx + s.sx; r.ey = s.cy + s.sy; r.ez = s.cz + s.sz;
@@ -840,13 +900,13 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
             travelled = fadd(travelled, 1.0f);
             last = !(travelled < lim);
         }
-        bool hb = false;  // the cell's bit, meaningful only while the step stays in the box
-        if (r.m) {
-            if (bx) r.bi = r.bi * one + r.sx;
-            if (by) r.bi = r.sy * four + r.bi;
-            if (bz) r.bi = r.sz * sixteen + r.bi;
-            hb = (r.m >> (r.bi & 63)) & 1;
-        }
+        // The cell's bit, meaningful only while the step stays in the box; in an empty box
+        // (m == 0) it is 0.  Testing it without a branch on m pays: nearly every warp has a
+        // lane inside a non-empty brick, so the branch would be taken anyway.
+        if (bx) r.bi = r.bi * one + r.sx;
+        if (by) r.bi = r.sy * four + r.bi;
+        if (bz) r.bi = r.sz * sixteen + r.bi;
+        const bool hb = (r.m >> (r.bi & 63)) & 1;
         if (((r.kx | r.ky | r.kz) < 0) | hb | last) {
             const int a = bx ? 0 : (by ? 1 : 2);
             const bool out = (r.kx | r.ky | r.kz) < 0;
@@ -855,7 +915,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
             if (out) {
                 refills++;
                 const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
-                const int t = enter_box(r, cx, cy, cz, P, alive, left);
+                const int t = DF ? enter_box(r, cx, cy, cz, P, alive, left) : enter_box_lean(r, cx, cy, cz, P, left);
                 if (t == T_HIT) { result = T_HIT; hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz; }
                 else if (t == T_MISS) result = T_MISS;
                 else result = T_LIVE;
@@ -926,9 +986,11 @@ __device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
 // render a world with depth-field words (the masks are its stop masks).
 template <bool EXACT, bool DEBUG, bool DF>
 __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_constant__ MaskParams P) {
-    __shared__ int2 alive[24];
-    fill_alive_ranges(alive, P, EXACT);
-    __syncthreads();
+    __shared__ int2 alive[24];  // read by enter_box, i.e. only with depth-field words
+    if (DF) {
+        fill_alive_ranges(alive, P, EXACT);
+        __syncthreads();
+    }
     const int tile = (int)blockIdx.x + P.tile0;
     const ViewDev& V = view_of(P, view_of_tile(P, tile));
     const int lt = tile - V.tile_begin;
