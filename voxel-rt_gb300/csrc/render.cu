@@ -806,7 +806,7 @@ __device__ __forceinline__ int enter_box_lean(BoxRay& r, int cx, int cy, int cz,
     const uint32_t bidx = (uint32_t)bx + (uint32_t)L.BWp * ((uint32_t)by + (uint32_t)L.BHp * (uint32_t)bz);
     const uint64_t m = __ldg(P.bricks + bidx);
     const int db = __ldg(P.bdir + (bidx * 8u + r.oct));
-    const int kk4 = m ? 0 : (max(db, 1) - 1) * P.four;
+    const int kk4 = (max(db, 1) - 1) * P.four;  // a non-empty brick has distance 0: its own box
     const int kmax = (int)__umulhi((unsigned)max(left, 0), 0x55555556u);  // floor(left / 3)
     r.kx = min(min((((r.sx > 0) ? ~cx : cx) & 3) + kk4, kcx), kmax);
     r.ky = min(min((((r.sy > 0) ? ~cy : cy) & 3) + kk4, kcy), kmax);
@@ -831,7 +831,7 @@ __device__ __forceinline__ int enter_box_lean(BoxRay& r, int cx, int cy, int cz,
 // then the shader's float test distTravelled < min(dist, RENDER_DIST) (:83), kept as a
 // float because the jumps make distTravelled fractional.  start_out receives the start
 // the hit position is measured from.
-template <bool DF>
+template <bool DF, bool COUNT>
 __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, V3 o, V3 d, int n, int maxSteps,
                                         float& cd, int& axis, int& sgn, int& steps, int32_t& hit_index,
                                         unsigned& refills, V3& start_out) {
@@ -913,7 +913,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
             const int left = r.lb + r.kx + r.ky + r.kz;
             left_end = left;
             if (out) {
-                refills++;
+                if (COUNT) refills++;  // box lookups, counted only for launches that report counters
                 const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
                 const int t = DF ? enter_box(r, cx, cy, cz, P, alive, left) : enter_box_lean(r, cx, cy, cz, P, left);
                 if (t == T_HIT) { result = T_HIT; hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz; }
@@ -982,8 +982,9 @@ __device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
 // One CTA per ray tile (tile_w x tile_h pixels, tile_w*tile_h == blockDim.x) over the tile
 // space of every view of the launch: a single frame, or a batch of cameras of any sizes.
 // EXACT launches (any view asking for step counts) step every ray to its end; DEBUG
-// launches (any view with a debug output) write the per-pixel side outputs; DF launches
-// render a world with depth-field words (the masks are its stop masks).
+// launches (any view with a debug output or counters) write the per-pixel side outputs
+// and count box lookups; DF launches render a world with depth-field words (the masks are
+// its stop masks).
 template <bool EXACT, bool DEBUG, bool DF>
 __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_constant__ MaskParams P) {
     __shared__ int2 alive[24];  // read by enter_box, i.e. only with depth-field words
@@ -1009,7 +1010,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
     V3 from = cam, from2;  // the start a hit position is measured from (moved by depth-field jumps)
     if (valid) {
         rd = primary_dir(u, px, py, V.width, V.height);
-        pr = cast_box<DF>(P, alive, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit, refills, from);
+        pr = cast_box<DF, DEBUG>(P, alive, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit, refills, from);
         res.primary_steps = steps;
     }
     const bool lit = valid && pr == T_HIT && u.viewDepthField != 1;
@@ -1062,7 +1063,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
                     }
                 }
                 if (cast) {
-                    const int sr = cast_box<DF>(P, alive, add3(hp, mul3s(dir, 0.001f)), dir, n, u.maxSteps, c2, a2,
+                    const int sr = cast_box<DF, DEBUG>(P, alive, add3(hp, mul3s(dir, 0.001f)), dir, n, u.maxSteps, c2, a2,
                                                 s2, steps, dummy, refills, from2);
                     const unsigned bit = 1u << (j + 1);
                     res.cast |= bit;
@@ -1270,10 +1271,13 @@ static int launch_tiles(const vrt_world* w, const ViewDev* h_views, int nviews, 
         P.cl[a] = exact ? 0 : std::max(0, std::min(P.bb[a], dims[a]));
         P.cl[3 + a] = exact ? dims[a] : std::min(dims[a], std::max(P.bb[3 + a] + 1, P.cl[a]));
     }
+    // DEBUG launches store side outputs and count box lookups: any view with a debug output
+    // or counters
     bool debug = false;
     for (int i = 0; i < nviews; i++) {
         const vrt_debug_out& d = h_views[i].dbg;
-        debug |= d.hit_index || d.cast_mask || d.occ_mask || d.steps || d.primary_steps || d.shade;
+        debug |= d.hit_index || d.cast_mask || d.occ_mask || d.steps || d.primary_steps || d.shade ||
+                 h_views[i].stats != nullptr;
     }
     const bool df = w->has_depth_field != 0;
     if (df) {
