@@ -243,7 +243,9 @@ int vrt_renderer_destroy(vrt_renderer* r);
  * 0 = bottom row (GL order); pixel (px,py) sees vPos = ((2px+1)/width-1, (2py+1)/height-1).  dbg,
  * d_stats and opts may be NULL.  The tile kernel's first render of a depth-field world
  * after its words changed also rebuilds the world's stop masks on this stream (allocated
- * on first use). */
+ * on first use, 16 bytes per brick).  The word kernel's first render after the words
+ * changed brings the world's z-major copy of the words up to date over the changed box
+ * on this stream (allocated and filled on first use: as large as the words). */
 int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32_t width,
                int32_t height, uint8_t* d_rgba, const vrt_debug_out* dbg, uint64_t* d_stats,
                const vrt_render_opts* opts, void* stream);

@@ -36,7 +36,10 @@ def test_reference_scene(cuda, oracle):
         assert int(f["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"]
 
 
-def test_edits_refresh_the_stop_masks(cuda, oracle, vrt_lib):
+@pytest.mark.parametrize("kernel", [vrt.KERNEL_MASK_PIXEL, vrt.KERNEL_WORD])
+def test_edits_refresh_the_stop_masks(cuda, oracle, vrt_lib, kernel):
+    """The tile kernel's stop masks and the word kernel's z-major copy of the words are
+    caches of the words: after each edit the next render sees the edited world."""
     W, H = 96, 48
     w = make_world(vrt_lib.terrain_generate(W, H, 17, 2), W, H)
     w.fix_depth_field()
@@ -52,7 +55,7 @@ def test_edits_refresh_the_stop_masks(cuda, oracle, vrt_lib):
         words = w.download(np.empty(W * H * W, np.int32))
         o = oracle.render(words, W, H, u, 80, 60)
         assert (o["hit"] >= 0).sum() > 100
-        assert_same_frame(o, gpu_render(w, u, 80, 60, kernel=vrt.KERNEL_MASK_PIXEL))
+        assert_same_frame(o, gpu_render(w, u, 80, 60, kernel=kernel))
         w.remove_sphere(40 + 9 * edit, 20, 40 - 7 * edit, 6, 1)  # with the depth-field refresh
 
 
@@ -107,9 +110,11 @@ def test_batch_on_a_depth_field_world(cuda, oracle):
     assert vrt.lib().vrt_render_batch_noalloc(arr, len(views), None, stream) == vrt.ESTATE
 
 
-def test_two_streams_after_an_edit(cuda, oracle, vrt_lib):
-    """The first render after an edit rebuilds the stop masks on its stream; a render of the
-    same world on another stream right after it must wait for that rebuild."""
+@pytest.mark.parametrize("kernel", [vrt.KERNEL_MASK_PIXEL, vrt.KERNEL_WORD])
+def test_two_streams_after_an_edit(cuda, oracle, vrt_lib, kernel):
+    """The first render after an edit rebuilds the stop masks (tile kernel) or updates the
+    z-major copy of the words (word kernel) on its stream; a render of the same world on
+    another stream right after it must wait for that."""
     import torch
     W, H = 96, 48
     w = make_world(vrt_lib.terrain_generate(W, H, 23, 2), W, H)
@@ -121,7 +126,7 @@ def test_two_streams_after_an_edit(cuda, oracle, vrt_lib):
     u.maxSteps = 200
     u.aspectRatio = 96 / 64
     o_opts = vrt.RenderOpts()
-    o_opts.kernel = vrt.KERNEL_MASK_PIXEL
+    o_opts.kernel = kernel
     r1, r2 = vrt.Renderer(), vrt.Renderer()
     s1, s2 = torch.cuda.Stream(), torch.cuda.Stream()
     for edit in range(3):
@@ -164,3 +169,37 @@ def test_banded_host_render_after_an_edit(cuda, oracle, vrt_lib):
         words = w.download(np.empty(W * H * W, np.int32))
         o = oracle.render(words, W, H, u, width, height)
         assert np.array_equal(host.numpy().reshape(height, width, 4), o["rgba"])
+
+
+def test_word_kernel_copy_follows_every_kind_of_edit(cuda, oracle, vrt_lib):
+    """The word kernel reads z steps from a z-major copy of the words, brought up to date
+    over the changed box at its next render: after placeVoxel, a partial upload, removeSphere
+    with the depth-field refresh and a fixDepthField box, each frame equals the oracle's on
+    the words of that moment, and the world's device bytes include the copy once."""
+    W, H = 80, 40
+    w = make_world(vrt_lib.terrain_generate(W, H, 29, 2), W, H)
+    w.fix_depth_field()
+    u = vrt.default_uniforms()
+    u.camPos[:] = [12.5, 34.25, 10.5]
+    u.rotateMatrix[:] = vrt.rotate_matrix(0.45, 0.7)  # looking along +z and +x, downwards
+    u.lightPos[:] = [40.0, 300.0, 60.0]
+    u.maxSteps = 160
+    u.aspectRatio = 72 / 48
+    before = w.info().device_bytes
+
+    def check():
+        words = w.download(np.empty(W * H * W, np.int32))
+        assert_same_frame(oracle.render(words, W, H, u, 72, 48), gpu_render(w, u, 72, 48, kernel=vrt.KERNEL_WORD))
+
+    check()  # makes the copy
+    assert w.info().device_bytes == before + 4 * W * H * W
+    w.place_voxel(30, 30, 34, 0x01FF0000)
+    check()
+    slab = np.full(W * 3, 0x0100FF00, np.int32)  # three rows of solid words at y = 26
+    w.upload(slab, first=26 * W + 40 * W * H)
+    check()
+    w.remove_sphere(36, 22, 40, 6, 1)
+    check()
+    w.fix_depth_field((20, 10, 20, 60, 40, 60))
+    check()
+    assert w.info().device_bytes == before + 4 * W * H * W

@@ -38,6 +38,7 @@ struct WordParams {
     int bb[6];   // solid bounding box: min x,y,z, max x,y,z (never smaller than the truth)
     int exact;   // 1: every DDA iteration of the shader runs (step counts asked for)
     int tw, th;  // pixel tile of a CTA (tw * th threads)
+    const int32_t* words_z;  // the same words with x and z swapped: z + W*y + W*H*x
 };
 
 // fl(i / 255) for i = 0..255: the shader's channel scale (fshader.glsl:184-186), filled on
@@ -136,10 +137,15 @@ __device__ WordRay cast_word(const int32_t* __restrict__ words, const Layout& L,
         if ((unsigned)r.cx >= (unsigned)L.W || (unsigned)(r.cy - lo_y) >= (unsigned)span_y ||
             (unsigned)r.cz >= (unsigned)L.W)
             break;  // getVoxelIndex == -1, or no solid voxel ahead
-        int32_t idx = r.cx + L.W * r.cy + L.W * L.H * r.cz;
-        int32_t v = __ldg(words + idx);
+        // A step along z reads the copy in which z is the fastest index: a run of z steps then
+        // reads consecutive words instead of one cache line per step (W*H words apart).  That
+        // run is the longest ray of the reference's own frame: the shader's x == y tie sends a
+        // ray along z for hundreds of steps, which set the frame's length.
+        const int32_t* q = axis == 2 ? p.words_z + (r.cz + L.W * r.cy + L.W * L.H * r.cx)
+                                     : words + (r.cx + L.W * r.cy + L.W * L.H * r.cz);
+        const int32_t v = __ldg(q);
         if (v >= 0) {
-            o.hit = idx;
+            o.hit = r.cx + L.W * r.cy + L.W * L.H * r.cz;
             break;
         } else if (v != -1) {  // depth-field jump
             float toJump = -__int_as_float(v);
@@ -1420,6 +1426,10 @@ int vrt_render(vrt_renderer* r, const vrt_world* w, const vrt_uniforms* u, int32
             return set_error(VRT_EINVAL, "pixel tile %dx%d: tile_w*tile_h must be a multiple of 32 up to 128", p.tw,
                              p.th);
         dim3 grid((width + p.tw - 1) / p.tw, (height + p.th - 1) / p.th);
+        // the z-major copy of the words is a cache of them, brought up to date here
+        st = refresh_words_z(const_cast<vrt_world*>(w), S(stream));
+        if (st) return st;
+        p.words_z = w->d_words_z;
         const bool debug = dbg && (dbg->hit_index || dbg->cast_mask || dbg->occ_mask || dbg->steps ||
                                    dbg->primary_steps || dbg->shade);
         if (debug) render_word_kernel<true><<<grid, threads, 0, S(stream)>>>(w->d_words, w->L, p);

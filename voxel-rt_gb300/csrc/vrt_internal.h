@@ -90,6 +90,11 @@ struct vrt_world {
     uint8_t* d_sdir = nullptr;      // directed brick distances over the stop masks
     bool stop_stale = true;         // the stop structures predate the last change of the words
     cudaEvent_t stop_ready = nullptr;  // recorded after each rebuild: renders on other streams wait on it
+    int32_t* d_words_z = nullptr;   // the word kernel's second copy of the words with x and z swapped
+                                    // (index z + W*y + W*H*x), made on first use
+    int z_dirty[6] = {0, 0, 0, 0, 0, 0};  // box [x0,x1)x[y0,y1)x[z0,z1) of words changed since the
+                                    // copy was last brought up to date (empty: x0 >= x1)
+    cudaEvent_t z_ready = nullptr;  // recorded after each copy update: renders on other streams wait on it
     uint8_t* d_tmp_a = nullptr;     // scratch of the distance passes (8 * n_bricks each)
     uint8_t* d_tmp_b = nullptr;
     int* d_flag = nullptr;          // has-depth-field flag written by the mask kernels
@@ -110,4 +115,8 @@ int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int 
 // Bring the stop masks and their directed distances up to date (allocated on first use),
 // and make stream s wait until they are: the rebuild may have run on another stream.
 int refresh_stop(vrt_world* w, cudaStream_t s);
+// Bring the z-major copy of the words up to date (allocated and filled on first use, then
+// only the box changed since), and make stream s wait until it is: the update may have
+// run on another stream.
+int refresh_words_z(vrt_world* w, cudaStream_t s);
 }  // namespace vrt

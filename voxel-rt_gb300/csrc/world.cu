@@ -288,12 +288,84 @@ int refresh_stop(vrt_world* w, cudaStream_t s) {
     return VRT_OK;
 }
 
+// The words of the box [x0,x1)x[y0,y1)x[z0,z1) changed: the z-major copy must follow there.
+static void mark_words_z(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int z1) {
+    int* b = w->z_dirty;
+    if (b[0] >= b[3]) {
+        b[0] = x0; b[1] = y0; b[2] = z0; b[3] = x1; b[4] = y1; b[5] = z1;
+        return;
+    }
+    b[0] = std::min(b[0], x0); b[1] = std::min(b[1], y0); b[2] = std::min(b[2], z0);
+    b[3] = std::max(b[3], x1); b[4] = std::max(b[4], y1); b[5] = std::max(b[5], z1);
+}
+
+// Whole-world copy with x and z swapped, through 32x32 tiles of the (x, z) plane of each y
+// so that both the reads (along x) and the writes (along z) are coalesced.
+__global__ void words_z_transpose_kernel(const int32_t* __restrict__ in, int32_t* __restrict__ out, Layout L) {
+    __shared__ int32_t tile[32][33];
+    const uint64_t W = L.W, WH = (uint64_t)L.W * L.H;
+    const int y = blockIdx.z;
+    const int x0 = blockIdx.x * 32, z0 = blockIdx.y * 32;
+    for (int j = threadIdx.y; j < 32; j += 8) {  // read: x along threadIdx.x
+        const int x = x0 + threadIdx.x, z = z0 + j;
+        if (x < L.W && z < L.W) tile[j][threadIdx.x] = in[x + W * y + WH * z];
+    }
+    __syncthreads();
+    for (int j = threadIdx.y; j < 32; j += 8) {  // write: z along threadIdx.x
+        const int z = z0 + threadIdx.x, x = x0 + j;
+        if (x < L.W && z < L.W) out[z + W * y + WH * x] = tile[threadIdx.x][j];
+    }
+}
+
+// The same for the words of one box (edit-sized), one thread per word.
+__global__ void words_z_box_kernel(const int32_t* __restrict__ in, int32_t* __restrict__ out, Layout L, int x0,
+                                   int y0, int z0, int nx, int ny, int nz) {
+    const uint64_t t = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= (uint64_t)nx * ny * nz) return;
+    const uint64_t W = L.W, WH = (uint64_t)L.W * L.H;
+    const uint64_t x = x0 + t % nx, y = y0 + (t / nx) % ny, z = z0 + t / ((uint64_t)nx * ny);
+    out[z + W * y + WH * x] = in[x + W * y + WH * z];
+}
+
+int refresh_words_z(vrt_world* w, cudaStream_t s) {
+    const Layout& L = w->L;
+    int* b = w->z_dirty;
+    if (w->d_words_z && b[0] >= b[3]) {
+        VRT_CUDA(cudaStreamWaitEvent(s, w->z_ready, 0));  // the last update, on whichever stream
+        return VRT_OK;
+    }
+    if (!w->d_words_z) {
+        cudaError_t e = cudaMalloc(&w->d_words_z, L.n_words * sizeof(int32_t));
+        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&w->z_ready, cudaEventDisableTiming);
+        if (e != cudaSuccess) {
+            cudaGetLastError();
+            cudaFree(w->d_words_z);
+            if (w->z_ready) cudaEventDestroy(w->z_ready);
+            w->d_words_z = nullptr;
+            w->z_ready = nullptr;
+            return set_error(VRT_ENOMEM, "z-major words: %s", cudaGetErrorString(e));
+        }
+        w->device_bytes += L.n_words * sizeof(int32_t);
+        dim3 grid((L.W + 31) / 32, (L.W + 31) / 32, L.H);
+        words_z_transpose_kernel<<<grid, dim3(32, 8), 0, s>>>(w->d_words, w->d_words_z, L);
+    } else {
+        const uint64_t n = (uint64_t)(b[3] - b[0]) * (b[4] - b[1]) * (b[5] - b[2]);
+        words_z_box_kernel<<<blocks_for(n, 256), 256, 0, s>>>(w->d_words, w->d_words_z, L, b[0], b[1], b[2],
+                                                               b[3] - b[0], b[4] - b[1], b[5] - b[2]);
+    }
+    VRT_CUDA(cudaGetLastError());
+    VRT_CUDA(cudaEventRecord(w->z_ready, s));
+    b[0] = b[3] = 0;
+    return VRT_OK;
+}
+
 int refresh_masks_box(vrt_world* w, int x0, int y0, int z0, int x1, int y1, int z1, cudaStream_t s) {
     const Layout& L = w->L;
     x0 = std::max(x0, 0); y0 = std::max(y0, 0); z0 = std::max(z0, 0);
     x1 = std::min(x1, L.W); y1 = std::min(y1, L.H); z1 = std::min(z1, L.W);
     if (x0 >= x1 || y0 >= y1 || z0 >= z1) return VRT_OK;
     w->stop_stale = true;
+    if (w->d_words_z) mark_words_z(w, x0, y0, z0, x1, y1, z1);
     int bx0 = x0 >> 2, by0 = y0 >> 2, bz0 = z0 >> 2;
     int bx1 = (x1 + 3) >> 2, by1 = (y1 + 3) >> 2, bz1 = (z1 + 3) >> 2;
     uint64_t nb = (uint64_t)(bx1 - bx0) * (by1 - by0) * (bz1 - bz0);
@@ -626,6 +698,8 @@ int vrt_world_destroy(vrt_world* w) {
     cudaFree(w->d_stop);
     cudaFree(w->d_sdir);
     if (w->stop_ready) cudaEventDestroy(w->stop_ready);
+    cudaFree(w->d_words_z);
+    if (w->z_ready) cudaEventDestroy(w->z_ready);
     cudaFree(w->d_tmp_a);
     cudaFree(w->d_tmp_b);
     cudaFree(w->d_flag);
