@@ -329,6 +329,9 @@ typedef struct vrt_server_config {
                                        by the kernel (the request's own host_rgba when it is
                                        page-locked and 4-byte aligned, else the slot's buffer);
                                        1 = device memory, copied to the slot's host buffer */
+    int32_t max_batch_pixels;       /* pixels per launch (0: no cap): a launch gathers requests while
+                                       their pixels stay within it (a larger request goes alone),
+                                       so that a request arriving under load waits behind less work */
 } vrt_server_config;
 
 #define VRT_REQ_RENDER 0

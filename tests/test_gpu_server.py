@@ -13,8 +13,8 @@ from helpers import gpu_render, make_world
 pytestmark = pytest.mark.gpu
 
 
-def make_server(budget=1 << 30, slots=3, max_batch=4, max_wait_us=0, image_memory=0):
-    cfg = vrt.ServerConfig(budget, slots, max_batch, max_wait_us, image_memory)
+def make_server(budget=1 << 30, slots=3, max_batch=4, max_wait_us=0, image_memory=0, max_batch_pixels=0):
+    cfg = vrt.ServerConfig(budget, slots, max_batch, max_wait_us, image_memory, max_batch_pixels)
     h = C.c_void_p()
     vrt.check(vrt.lib().vrt_server_create(C.byref(cfg), C.byref(h)))
     return h
@@ -139,7 +139,7 @@ def test_edits_are_ordered_within_a_world(cuda, worlds):
 
 def test_bad_configs_are_refused(cuda):
     for cfg in [(1 << 30, 0, 4, 0, 0), (1 << 30, 3, 0, 0, 0), (0, 3, 4, 0, 0), (1 << 30, 3, 4, -1, 0),
-                (1 << 30, 3, 4, 0, 2)]:
+                (1 << 30, 3, 4, 0, 2), (1 << 30, 3, 4, 0, 0, -1)]:
         h = C.c_void_p()
         assert vrt.lib().vrt_server_create(C.byref(vrt.ServerConfig(*cfg)), C.byref(h)) == vrt.EINVAL, cfg
         assert not h.value
@@ -235,4 +235,31 @@ def test_partial_batch_waits_for_company(cuda, worlds):
     assert done[4].start_ms - done[4].submit_ms >= 29.0
     for img in imgs:
         assert np.array_equal(img.reshape(32, 32, 4), alone)
+    vrt.lib().vrt_server_destroy(srv)
+
+
+def test_pixel_cap_splits_launches(cuda, worlds):
+    """max_batch_pixels: a launch gathers requests only while their pixels fit the cap (a
+    larger request goes alone); every image still equals the one rendered alone."""
+    _, b = worlds
+    w = make_world(b.words, b.W, b.H)
+    u = vrt.Uniforms.from_buffer_copy(b.uniforms)
+    u.aspectRatio = 1.0
+    sizes = [32, 32, 32, 32, 32, 80, 32]  # 1024-pixel requests and one of 6400
+    alone = {n: gpu_render(w, u, n, n)["rgba"] for n in set(sizes)}
+    srv = make_server(slots=1, max_batch=8, max_batch_pixels=2 * 32 * 32)
+    wid = add_world(srv, w)
+    imgs = [np.zeros(n * n * 4, np.uint8) for n in sizes]
+    for i, n in enumerate(sizes):
+        submit_render(srv, wid, u, n, n, imgs[i], i)
+    done = collect(srv, len(sizes))
+    launches = {}
+    for tag, c in done.items():
+        assert c.status == 0
+        launches.setdefault(c.start_ms, []).append(sizes[tag])
+    for members in launches.values():
+        assert sum(m * m for m in members) <= 2 * 32 * 32 or len(members) == 1, launches
+    assert any(members == [80] for members in launches.values())
+    for i, n in enumerate(sizes):
+        assert np.array_equal(imgs[i].reshape(n, n, 4), alone[n]), f"request {i}"
     vrt.lib().vrt_server_destroy(srv)

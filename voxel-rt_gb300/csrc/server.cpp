@@ -8,7 +8,8 @@
 //     memory budget (resident worlds + images in flight) allows;
 //   - batches the renders of one world into one launch (vrt_render_batch), so requests
 //     that arrive while others run join the next free slot and overlap them on the device;
-//     a partial batch may wait max_wait_us for company;
+//     a partial batch may wait max_wait_us for company, and max_batch_pixels caps a launch's
+//     work so that a request arriving under load waits behind less of it;
 //   - keeps the order of each world's requests: an edit waits (on the device, through
 //     events) for every earlier render of its world, and later renders wait for it.
 // Requests larger than the whole budget complete with VRT_EBUDGET.
@@ -289,6 +290,14 @@ static int launch_renders(vrt_server* s, int si, std::vector<Queued>& batch) {
     return VRT_OK;
 }
 
+static inline uint64_t pixels_of(const vrt_request& r) { return (uint64_t)r.width * (uint64_t)r.height; }
+
+// Would a batch of n requests and px pixels exceed max_batch_pixels by taking r?  The first
+// request of a batch always fits.
+static inline bool over_pixel_cap(const vrt_server* s, int n, uint64_t px, const vrt_request& r) {
+    return s->cfg.max_batch_pixels > 0 && n > 0 && px + pixels_of(r) > (uint64_t)s->cfg.max_batch_pixels;
+}
+
 // Take the next launch off the queue for a free slot; returns false when nothing can start.
 static bool admit(vrt_server* s, int si, int* status) {
     std::vector<Queued> batch;
@@ -318,13 +327,15 @@ static bool admit(vrt_server* s, int si, int* status) {
                 // a young partial batch waits for company (a full one, or one that meets the
                 // world's next edit, goes now)
                 int n = 0;
+                uint64_t px = 0;
                 bool closed = false;
                 for (auto jt = it; jt != s->queue.end() && n < s->cfg.max_batch; ++jt) {
                     if (jt->req.world_id != wid) continue;
-                    if (jt->req.kind == VRT_REQ_EDIT) {
-                        closed = true;
+                    if (jt->req.kind == VRT_REQ_EDIT || over_pixel_cap(s, n, px, jt->req)) {
+                        closed = true;  // the batch cannot grow any further
                         break;
                     }
+                    px += pixels_of(jt->req);
                     n++;
                 }
                 if (n < s->cfg.max_batch && !closed) {
@@ -333,12 +344,14 @@ static bool admit(vrt_server* s, int si, int* status) {
                 }
             }
             // gather this world's renders in order, up to the first edit of the world
-            uint64_t used = s->image_bytes;
+            uint64_t used = s->image_bytes, px = 0;
             for (auto jt = it; jt != s->queue.end() && (int)batch.size() < s->cfg.max_batch;) {
                 if (jt->req.world_id != wid) { ++jt; continue; }
                 if (jt->req.kind == VRT_REQ_EDIT) break;
                 if (used + jt->bytes > cap) break;
+                if (over_pixel_cap(s, (int)batch.size(), px, jt->req)) break;
                 used += jt->bytes;
+                px += pixels_of(jt->req);
                 batch.push_back(*jt);
                 jt = s->queue.erase(jt);
             }
@@ -366,8 +379,9 @@ int vrt_server_create(const vrt_server_config* cfg, vrt_server** out) {
     if (!cfg || !out) return set_error(VRT_EINVAL, "NULL argument");
     *out = nullptr;
     if (cfg->slots < 1 || cfg->slots > 64 || cfg->max_batch < 1 || cfg->memory_budget_bytes == 0 ||
-        cfg->max_wait_us < 0 || (cfg->image_memory != 0 && cfg->image_memory != 1))
+        cfg->max_wait_us < 0 || (cfg->image_memory != 0 && cfg->image_memory != 1) || cfg->max_batch_pixels < 0)
         return set_error(VRT_EINVAL, "bad server config (slots 1-64, max_batch >= 1, budget > 0, max_wait_us >= 0, "
+                                     "max_batch_pixels >= 0, "
                                      "image_memory 0 or 1)");
     vrt_server* s = new vrt_server();
     s->cfg = *cfg;

@@ -24,8 +24,8 @@ RESOLUTIONS = [(640, 360), (1280, 720), (1920, 1080)]
 
 class Server:
     def __init__(self, budget_bytes: int, slots: int = 4, max_batch: int = 8, max_wait_us: int = 0,
-                 image_memory: int = 0):
-        cfg = vrt.ServerConfig(budget_bytes, slots, max_batch, max_wait_us, image_memory)
+                 image_memory: int = 0, max_batch_pixels: int = 0):
+        cfg = vrt.ServerConfig(budget_bytes, slots, max_batch, max_wait_us, image_memory, max_batch_pixels)
         self.h = C.c_void_p()
         vrt.check(vrt.lib().vrt_server_create(C.byref(cfg), C.byref(self.h)))
         self._buf = (vrt.Completion * 512)()

@@ -116,6 +116,7 @@ class ServerConfig(C.Structure):
         ("max_batch", C.c_int32),
         ("max_wait_us", C.c_int32),
         ("image_memory", C.c_int32),
+        ("max_batch_pixels", C.c_int32),
     ]
 
 
