@@ -535,6 +535,9 @@ def bench_stress(vrt, torch, scenes, dev, stream):
     return res
 
 
+SERVED_BATCH_PIXELS = 1920 * 1080
+
+
 def bench_served(vrt, torch, scenes, sc, full_world):
     """4 resident worlds (256^3, 512x256x512, 1024x256x1024 x2), Poisson arrivals."""
     import serving
@@ -548,10 +551,12 @@ def bench_served(vrt, torch, scenes, sc, full_world):
             w.upload(s.words)
             s.words = None
         specs.append(serving.WorldSpec(s, w))
-    srv = serving.Server(40 << 30, slots=4, max_batch=8)
+    # a launch takes up to 8 requests and at most one 1080p frame of pixels, so that a request
+    # arriving under load waits behind at most about one frame of work per slot
+    srv = serving.Server(40 << 30, slots=4, max_batch=8, max_batch_pixels=SERVED_BATCH_PIXELS)
     wids = [srv.add_world(s.world) for s in specs]
     results = []
-    for rate in (250.0, 1000.0, 4000.0, 16000.0):
+    for rate in (250.0, 1000.0, 4000.0, 8000.0, 16000.0):
         reqs = serving.make_requests(specs, rate, 1.0, seed=int(rate))
         done, wall = serving.run_open_loop(srv, wids, reqs)
         res = serving.summarize(done, wall)
@@ -588,7 +593,8 @@ def bench_served(vrt, torch, scenes, sc, full_world):
     full_world.upload(sc.words)  # the served edits changed the shared world: restore it
     sat = max(x["mrays_per_s"] for x in results if "mrays_per_s" in x)
     return {"worlds": ["256x256x256", "512x256x512", "1024x256x1024", "1024x256x1024"], "budget_gib": 40,
-            "slots": 4, "max_batch": 8, "images": "page-locked host memory, stored by the render kernel",
+            "slots": 4, "max_batch": 8, "max_batch_pixels": SERVED_BATCH_PIXELS,
+            "images": "page-locked host memory, stored by the render kernel",
             "sweep": results,
             "plain_sync": {"renders": n_render, "seconds": plain_s, "mrays_per_s": plain_rays / plain_s / 1e6,
                            "ms_per_render": plain_s * 1e3 / max(n_render, 1)},

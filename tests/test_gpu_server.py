@@ -263,3 +263,44 @@ def test_pixel_cap_splits_launches(cuda, worlds):
     for i, n in enumerate(sizes):
         assert np.array_equal(imgs[i].reshape(n, n, 4), alone[n]), f"request {i}"
     vrt.lib().vrt_server_destroy(srv)
+
+
+def test_add_world_while_another_thread_polls(cuda, worlds):
+    """vrt_server_add_world may run on another thread while this one submits and polls: the
+    world list grows under the server's lock and entries never move, so renders of the
+    first world keep their results while worlds are being added."""
+    import threading
+    a, b = worlds
+    w0 = make_world(b.words, b.W, b.H)
+    extra = [make_world(b.words, b.W, b.H) for _ in range(24)]
+    u = vrt.Uniforms.from_buffer_copy(b.uniforms)
+    u.aspectRatio = 1.0
+    alone = gpu_render(w0, u, 40, 40)["rgba"]
+    srv = make_server(budget=8 << 30, slots=3, max_batch=2)
+    wid = add_world(srv, w0)
+    ids = []
+
+    def adder():
+        for w in extra:
+            ids.append(add_world(srv, w))
+
+    t = threading.Thread(target=adder)
+    imgs = [np.zeros(40 * 40 * 4, np.uint8) for _ in range(40)]
+    buf = (vrt.Completion * 64)()
+    got = []
+    t.start()
+    for i, img in enumerate(imgs):
+        submit_render(srv, wid, u, 40, 40, img, i)
+        got += [buf[k] for k in range(vrt.check(vrt.lib().vrt_server_poll(srv, buf, 64)))]
+    t.join()
+    vrt.check(vrt.lib().vrt_server_drain(srv))
+    while True:
+        k = vrt.check(vrt.lib().vrt_server_poll(srv, buf, 64))
+        got += [buf[i] for i in range(k)]
+        if k == 0:
+            break
+    assert sorted(ids) == list(range(1, 25))
+    assert len(got) == len(imgs) and all(c.status == 0 for c in got)
+    for img in imgs:
+        assert np.array_equal(img.reshape(40, 40, 4), alone)
+    vrt.lib().vrt_server_destroy(srv)
