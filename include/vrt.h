@@ -231,9 +231,12 @@ int vrt_terrain_height(int32_t width, uint64_t seed, int32_t x, int32_t z);
 
 /* ---- rendering ---- */
 /* A renderer owns per-launch scratch: the view table of batches, the persistent kernel's
- * tile counter, the staging image and streams of vrt_render_to_host.  Creating the first
- * renderer on a device also fills a 1 KiB table the pixel colour reads (synchronises the
- * device once).  One renderer per concurrently used stream. */
+ * tile counter, the staging image and streams of vrt_render_to_host, and the word
+ * kernel's tile order (128 bytes per pixel tile).  Each word-kernel render sorts its tiles
+ * into cost classes as they end, and the next word-kernel render of the same tile grid on
+ * the same renderer launches them heaviest class first; the order changes no result.
+ * Creating the first renderer on a device also fills a 1 KiB table the pixel colour reads
+ * (synchronises the device once).  One renderer per concurrently used stream. */
 int vrt_renderer_create(vrt_renderer** out);
 int vrt_renderer_destroy(vrt_renderer* r);
 

@@ -203,3 +203,34 @@ def test_word_kernel_copy_follows_every_kind_of_edit(cuda, oracle, vrt_lib):
     w.fix_depth_field((20, 10, 20, 60, 40, 60))
     check()
     assert w.info().device_bytes == before + 4 * W * H * W
+
+
+def test_word_kernel_launches_heaviest_tiles_first(cuda, oracle):
+    """Each word-kernel render records its tiles' costs, and the next render of the same
+    grid on the same renderer launches the tiles heaviest first.  The order moves tiles,
+    not results: the first (row order) and the later (ordered) frames of the reference
+    scene equal the oracle's, also after the camera moved (an order from the old view),
+    when the tile grid changes (the order starts over) and with every debug output."""
+    case = load_golden("shader_reference_scene.npz")
+    w = vrt.World(512, 96)
+    w.init_reference()
+    w.fix_depth_field()
+    words = w.download(np.empty(512 * 96 * 512, np.int32))
+    u = uniforms_from_dict(json.loads(str(case["uniforms"])))
+    r = vrt.Renderer()
+    o = oracle.render(words, 512, 96, u, 800, 600)
+    for _ in range(3):
+        f = gpu_render(w, u, 800, 600, kernel=vrt.KERNEL_WORD, debug=False, renderer=r)
+        assert np.array_equal(f["rgba"], o["rgba"])
+        assert int(f["stats"][vrt.STAT_RAYS]) == o["totals"]["rays"]
+        assert int(f["stats"][vrt.STAT_PIXELS]) == 800 * 600
+    u2 = uniforms_from_dict(json.loads(str(case["uniforms"])))
+    u2.camPos[:] = [300.5, 62.25, 90.75]
+    u2.rotateMatrix[:] = vrt.rotate_matrix(-0.2, 2.4)
+    o2 = oracle.render(words, 512, 96, u2, 800, 600)
+    for tile in (None, None, (8, 16), (8, 16), (32, 4)):
+        f = gpu_render(w, u2, 800, 600, kernel=vrt.KERNEL_WORD, debug=False, renderer=r, tile=tile)
+        assert np.array_equal(f["rgba"], o2["rgba"]), tile
+        assert int(f["stats"][vrt.STAT_RAYS]) == o2["totals"]["rays"], tile
+    assert_same_frame(o2, gpu_render(w, u2, 800, 600, kernel=vrt.KERNEL_WORD, renderer=r, tile=(32, 4)))
+    r.close()
