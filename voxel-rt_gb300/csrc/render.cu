@@ -768,16 +768,17 @@ __global__ void __launch_bounds__(kThreads, MINB) render_mask_kernel(const __gri
 // ---------------------------------------------------------------- tile kernel, one thread per pixel
 
 // Where a ray stands inside its known box.  Per axis: k = further steps along that axis
-// that stay inside the box (the step that makes k negative leaves it), e = the cell
-// coordinate that step reaches, so the cell is always e - s*(k+1).  An axis the ray does
-// not move along (s == 0) has k = INT_MAX and e = its fixed cell.
+// that stay inside the box (the step that makes k negative leaves it), e = the box's last
+// cell along that axis, the one k further steps reach, so the current cell is always
+// e - s*k (one multiply-add).  An axis the ray does not move along (s == 0) has
+// k = INT_MAX and e = its fixed cell.
 struct BoxRay {
     float tx, ty, tz;
     float dx, dy, dz;
     int kx, ky, kz;
     int ex, ey, ez;
     int sx, sy, sz;
-    uint32_t oct;    // octant of travel: bit a set when s_a > 0
+    int sc;          // sign code (sx+1) + 3(sy+1) + 9(sz+1): the ray's entry of clip_k
     int lb;          // lb + kx + ky + kz = DDA iterations left after the current one (negative on
                      // the last allowed one): every iteration lowers exactly one k
     int bi;          // bit of the current cell in m (valid while m != 0)
@@ -785,13 +786,13 @@ struct BoxRay {
 };
 
 // kmax limits k: a box is cut short so that the ray leaves it by its last allowed
-// iteration (see cast_box).  e = c + s * (k + 1) is the first cell past the (possibly
-// nearer) far face; k = s * (ee - c) - 1 and e are multiply-adds, which issue on the FMA
-// pipe rather than the integer/logic pipe.
+// iteration (see cast_box).  e = c + s * k is the last cell before the (possibly nearer)
+// far face; k = s * (ee - c) - 1 and e are multiply-adds, which issue on the FMA pipe
+// rather than the integer/logic pipe.
 __device__ __forceinline__ void set_axis(int c, int s, int lo, int hi, int kmax, int& k, int& e) {
     const int ee = s > 0 ? hi : lo - 1;
     k = min(s != 0 ? s * (ee - c) - 1 : INT_MAX, kmax);
-    e = s * (k + 1) + c;
+    e = s * k + c;
 }
 
 // Per-octant alive ranges of a launch, one (lo, span) pair per octant and axis: a cell
@@ -830,9 +831,10 @@ __device__ __forceinline__ void fill_alive_ranges(int2* alive, const MaskParams&
 // the step cap is then tested only when a box is left.
 // Returns T_LIVE, T_HIT (c is solid) or T_MISS (c is outside the alive ranges).
 __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, const MaskParams& P,
-                                         const int2* alive, int left) {
+                                         const int2* alive, const int4* clip_k, int left) {
     const Layout& L = P.L;
-    const int2 ax = alive[r.oct * 3], ay = alive[r.oct * 3 + 1], az = alive[r.oct * 3 + 2];
+    const int oct = clip_k[r.sc].w;
+    const int2 ax = alive[oct * 3], ay = alive[oct * 3 + 1], az = alive[oct * 3 + 2];
     if ((unsigned)(cx - ax.x) >= (unsigned)ax.y || (unsigned)(cy - ay.x) >= (unsigned)ay.y ||
         (unsigned)(cz - az.x) >= (unsigned)az.y)
         return T_MISS;
@@ -841,7 +843,7 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
     const uint32_t bidx = (uint32_t)bx + (uint32_t)L.BWp * ((uint32_t)by + (uint32_t)L.BHp * (uint32_t)bz);
     // the two loads are independent: issue them together, wait once
     const uint64_t m = __ldg(P.bricks + bidx);
-    const int db = __ldg(P.bdir + (bidx * 8u + r.oct));
+    const int db = __ldg(P.bdir + (bidx * 8u + oct));
     const int k = m ? 0 : max(db, 1) - 1;
     // clip to the world, and for inexact launches to the solid box too: a ray that
     // leaves the solid box along its direction of travel then ends at the next lookup.
@@ -866,37 +868,37 @@ __device__ __forceinline__ int enter_box(BoxRay& r, int cx, int cy, int cz, cons
 // world (and of the clip box along an axis the ray does not move along) once; every later
 // cell lies on the inner side of those bounds, so here only the far side of the clip box
 // [cl[0], cl[3]) x [cl[1], cl[4]) x [cl[2], cl[5]) can end the ray:
-//   kclip = s > 0 ? hi - 1 - c : c - lo     (steps before the far clip face; INT_MAX if s == 0)
-// kclip < 0 along some axis: the cell is beyond that face (outside the world, or beyond
-// the solid box in the direction of travel), which ends the ray as a miss.  Otherwise the
-// box along each axis is the rest of the brick plus 4 cells per further brick of an empty
-// cube, cut at the clip face and the step cap:
+//   kclip = s > 0 ? hi - 1 - c : (s < 0 ? c - lo : INT_MAX)   (steps before the far clip face)
+//         = A - s * c,   A = hi - 1, -lo or INT_MAX
+// A depends only on the ray's signs: clip_k holds it for each of the 27 sign codes (with
+// the octant, which indexes the directed distances), so the three terms are one shared
+// load and three multiply-adds.  kclip < 0 along some axis: the cell is beyond that face
+// (outside the world, or beyond the solid box in the direction of travel), which ends the
+// ray as a miss.  Otherwise the box along each axis is the rest of the brick plus 4 cells
+// per further brick of an empty cube, cut at the clip face and the step cap:
 //   k = min((s > 0 ? 3 - (c & 3) : c & 3) + 4 kk, kclip, kmax)
 // which is enter_box's box without its near-side bounds.  (An axis the ray does not move
 // along steps only when its intersect is -inf or NaN; its cell stays put and its k only
-// decides how often the box is looked up again.)  This is about 20 instructions shorter
-// than enter_box, and the box lookup runs in nearly every warp iteration.
-__device__ __forceinline__ int clip_far(int s, int c, int lo, int hi) {
-    return s > 0 ? hi - 1 - c : (s < 0 ? c - lo : INT_MAX);
-}
-__device__ __forceinline__ int enter_box_lean(BoxRay& r, int cx, int cy, int cz, const MaskParams& P, int left) {
+// decides how often the box is looked up again.)  A lookup runs in about a quarter of the
+// loop's warp iterations, with some 25 lanes at once, so each instruction here counts.
+__device__ __forceinline__ int enter_box_lean(BoxRay& r, int cx, int cy, int cz, const MaskParams& P,
+                                              const int4* clip_k, int left) {
     const Layout& L = P.L;
-    const int kcx = clip_far(r.sx, cx, P.cl[0], P.cl[3]);
-    const int kcy = clip_far(r.sy, cy, P.cl[1], P.cl[4]);
-    const int kcz = clip_far(r.sz, cz, P.cl[2], P.cl[5]);
+    const int4 A = clip_k[r.sc];
+    const int kcx = A.x - r.sx * cx, kcy = A.y - r.sy * cy, kcz = A.z - r.sz * cz;
     if ((kcx | kcy | kcz) < 0) return T_MISS;
     const int bx = cx >> 2, by = cy >> 2, bz = cz >> 2;
     const uint32_t bidx = (uint32_t)bx + (uint32_t)L.BWp * ((uint32_t)by + (uint32_t)L.BHp * (uint32_t)bz);
     const uint64_t m = __ldg(P.bricks + bidx);
-    const int db = __ldg(P.bdir + (bidx * 8u + r.oct));
+    const int db = __ldg(P.bdir + (bidx * 8u + A.w));
     const int kk4 = (max(db, 1) - 1) * P.four;  // a non-empty brick has distance 0: its own box
     const int kmax = (int)__umulhi((unsigned)max(left, 0), 0x55555556u);  // floor(left / 3)
     r.kx = min(min((((r.sx > 0) ? ~cx : cx) & 3) + kk4, kcx), kmax);
     r.ky = min(min((((r.sy > 0) ? ~cy : cy) & 3) + kk4, kcy), kmax);
     r.kz = min(min((((r.sz > 0) ? ~cz : cz) & 3) + kk4, kcz), kmax);
-    r.ex = r.sx * (r.kx + 1) + cx;
-    r.ey = r.sy * (r.ky + 1) + cy;
-    r.ez = r.sz * (r.kz + 1) + cz;
+    r.ex = r.sx * r.kx + cx;
+    r.ey = r.sy * r.ky + cy;
+    r.ez = r.sz * r.kz + cz;
     r.lb = left - (r.kx + r.ky + r.kz);
     r.m = m;
     r.bi = (cx & 3) | ((cy & 3) << 2) | ((cz & 3) << 4);
@@ -915,7 +917,8 @@ __device__ __forceinline__ int enter_box_lean(BoxRay& r, int cx, int cy, int cz,
 // float because the jumps make distTravelled fractional.  start_out receives the start
 // the hit position is measured from.
 template <bool DF, bool COUNT>
-__device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, V3 o, V3 d, int n, int maxSteps,
+__device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, const int4* clip_k, V3 o, V3 d,
+                                        int n, int maxSteps,
                                         float& cd, int& axis, int& sgn, int& steps, int32_t& hit_index,
                                         unsigned& refills, V3& start_out) {
     start_out = o;
@@ -925,7 +928,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
     r.tx = s.tx; r.ty = s.ty; r.tz = s.tz;
     r.dx = s.dx; r.dy = s.dy; r.dz = s.dz;
     r.sx = s.sx; r.sy = s.sy; r.sz = s.sz;
-    r.oct = (s.sx > 0) | ((s.sy > 0) << 1) | ((s.sz > 0) << 2);
+    r.sc = (s.sx + 1) + 3 * (s.sy + 1) + 9 * (s.sz + 1);
     const int n0 = max(0, min(n, maxSteps));
     if (n0 == 0) return T_MISS;
     // The bit-index updates are multiply-adds by kernel parameters equal to 1, 4 and 16.
@@ -967,7 +970,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
     }
     // no box yet: the first step along any axis (even one with s == 0) triggers a lookup
     r.kx = 0; r.ky = 0; r.kz = 0;
-    r.ex = s.cx + s.sx; r.ey = s.cy + s.sy; r.ez = s.cz + s.sz;
+    r.ex = s.cx; r.ey = s.cy; r.ez = s.cz;
     r.m = 0;
     r.bi = 0;
     int result = T_MISS;
@@ -997,14 +1000,15 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
             left_end = left;
             if (out) {
                 if (COUNT) refills++;  // box lookups, counted only for launches that report counters
-                const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
-                const int t = DF ? enter_box(r, cx, cy, cz, P, alive, left) : enter_box_lean(r, cx, cy, cz, P, left);
+                const int cx = r.ex - r.sx * r.kx, cy = r.ey - r.sy * r.ky, cz = r.ez - r.sz * r.kz;
+                const int t = DF ? enter_box(r, cx, cy, cz, P, alive, clip_k, left)
+                                 : enter_box_lean(r, cx, cy, cz, P, clip_k, left);
                 if (t == T_HIT) { result = T_HIT; hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz; }
                 else if (t == T_MISS) result = T_MISS;
                 else result = T_LIVE;
             } else if (hb) {
                 result = T_HIT;
-                const int cx = r.ex - r.sx * (r.kx + 1), cy = r.ey - r.sy * (r.ky + 1), cz = r.ez - r.sz * (r.kz + 1);
+                const int cx = r.ex - r.sx * r.kx, cy = r.ey - r.sy * r.ky, cz = r.ez - r.sz * r.kz;
                 hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz;
             } else {
                 result = T_MISS;  // DF: the float cap, this was the last iteration
@@ -1023,7 +1027,7 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
                     // no box yet: the first step from the new cell looks one up
                     r.kx = 0; r.ky = 0; r.kz = 0;
                     r.lb = left;
-                    r.ex = ncx + r.sx; r.ey = ncy + r.sy; r.ez = ncz + r.sz;
+                    r.ex = ncx; r.ey = ncy; r.ez = ncz;
                     r.m = 0;
                     r.bi = 0;
                     hit_index = -1;
@@ -1071,10 +1075,18 @@ __device__ __forceinline__ int view_of_tile(const MaskParams& P, int t) {
 template <bool EXACT, bool DEBUG, bool DF>
 __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_constant__ MaskParams P) {
     __shared__ int2 alive[24];  // read by enter_box, i.e. only with depth-field words
-    if (DF) {
-        fill_alive_ranges(alive, P, EXACT);
-        __syncthreads();
+    __shared__ int4 clip_k[27];  // per sign code: the far-clip constants of enter_box_lean, and the octant
+    if (DF) fill_alive_ranges(alive, P, EXACT);
+    if (threadIdx.x < 27) {
+        const int t = threadIdx.x, sx = t % 3 - 1, sy = (t / 3) % 3 - 1, sz = t / 9 - 1;
+        int4 c;
+        c.x = sx > 0 ? P.cl[3] - 1 : (sx < 0 ? -P.cl[0] : INT_MAX);
+        c.y = sy > 0 ? P.cl[4] - 1 : (sy < 0 ? -P.cl[1] : INT_MAX);
+        c.z = sz > 0 ? P.cl[5] - 1 : (sz < 0 ? -P.cl[2] : INT_MAX);
+        c.w = (sx > 0) | ((sy > 0) << 1) | ((sz > 0) << 2);
+        clip_k[t] = c;
     }
+    __syncthreads();
     const int tile = (int)blockIdx.x + P.tile0;
     const ViewDev& V = view_of(P, view_of_tile(P, tile));
     const int lt = tile - V.tile_begin;
@@ -1093,7 +1105,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
     V3 from = cam, from2;  // the start a hit position is measured from (moved by depth-field jumps)
     if (valid) {
         rd = primary_dir(u, px, py, V.width, V.height);
-        pr = cast_box<DF, DEBUG>(P, alive, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit, refills, from);
+        pr = cast_box<DF, DEBUG>(P, alive, clip_k, cam, rd, u.maxSteps, u.maxSteps, cd, axis, sgn, steps, hit, refills, from);
         res.primary_steps = steps;
     }
     const bool lit = valid && pr == T_HIT && u.viewDepthField != 1;
@@ -1146,7 +1158,7 @@ __global__ void __launch_bounds__(128, 8) render_tiles_kernel(const __grid_const
                     }
                 }
                 if (cast) {
-                    const int sr = cast_box<DF, DEBUG>(P, alive, add3(hp, mul3s(dir, 0.001f)), dir, n, u.maxSteps, c2, a2,
+                    const int sr = cast_box<DF, DEBUG>(P, alive, clip_k, add3(hp, mul3s(dir, 0.001f)), dir, n, u.maxSteps, c2, a2,
                                                 s2, steps, dummy, refills, from2);
                     const unsigned bit = 1u << (j + 1);
                     res.cast |= bit;
