@@ -60,6 +60,17 @@ def test_zero_component_gets_stuck(oracle):
     assert hit == idx(8, 8, 8) and steps == 1  # ... and a solid start cell is hit at once
 
 
+def test_nan_intersects_step_z_for_good(oracle):
+    """dir = +z exactly from (8, 8, 0.5): tx = ty = (8 - 8.0) / 0 = NaN, so neither x nor y
+    is ever strictly smallest (fshader.glsl:87-104) and z is stepped until the voxel.  From
+    the voxel's face toward +y, the x and z intersects are NaN and the z step is 0: the
+    ray re-tests the voxel it starts in and hits it."""
+    hit, _, _, steps = oracle.cast_ray(world([(8, 8, 12)]), S, S, [8.0, 8.0, 0.5], [0.0, 0.0, 1.0], 50, 50)
+    assert hit == idx(8, 8, 12) and steps == 12
+    hit, _, _, steps = oracle.cast_ray(world([(8, 8, 12)]), S, S, [8.0, 8.001, 12.0], [0.0, 1.0, 0.0], 50, 50)
+    assert hit == idx(8, 8, 12) and steps == 1
+
+
 def test_step_cap_and_dist(oracle):
     d = nrm([0.3, 0.2, 1.0])
     for dist, cap, want in [(100, 3, 3), (2, 100, 2), (0, 100, 0), (100, 0, 0)]:
@@ -218,6 +229,17 @@ def kat_scenes():
     u.aspectRatio = 1.0
     u.maxSteps = 40
     scenes.append(("zero-dir", world([(8, 8, 12), (3, 3, 3), (8, 1, 9)]), u, 17, 9))
+    # a start on integer coordinates along zero direction components: (c - start) / 0 = 0/0,
+    # NaN intersects, so neither x nor y is ever strictly smallest and z is stepped for good
+    # (fshader.glsl:87-104).  The centre pixel's ray runs along +z from (8, 8, 0.5) to the
+    # voxel (8, 8, 12); its shadow ray toward (8, 40, 12) has NaN x and z intersects and a
+    # zero z step, so it re-tests the hit voxel itself and is occluded.
+    u = vrt.default_uniforms()
+    u.camPos[:] = [8.0, 8.0, 0.5]
+    u.lightPos[:] = [8.0, 40.0, 12.0]
+    u.aspectRatio = 17 / 9
+    u.maxSteps = 40
+    scenes.append(("nan-dir", world([(8, 8, 12), (8, 7, 9), (3, 3, 3)]), u, 17, 9))
     # exact ties on the diagonal
     u = vrt.default_uniforms()
     u.camPos[:] = [0.5, 0.5, 0.5]

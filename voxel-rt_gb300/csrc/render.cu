@@ -1017,9 +1017,8 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
                 const int cx = r.ex - r.sx * r.kx, cy = r.ey - r.sy * r.ky, cz = r.ez - r.sz * r.kz;
                 const int t = DF ? enter_box(r, cx, cy, cz, P, alive, clip_k, left)
                                  : enter_box_lean(r, cx, cy, cz, P, clip_k, left);
-                if (t == T_HIT) { result = T_HIT; hit_index = cx + P.L.W * cy + P.L.W * P.L.H * cz; }
-                else if (t == T_MISS) result = T_MISS;
-                else result = T_LIVE;
+                result = t;  // T_LIVE, T_HIT or T_MISS, taken as is: no branch on it
+                hit_index = t == T_HIT ? cx + P.L.W * cy + P.L.W * P.L.H * cz : hit_index;
             } else if (hb) {
                 result = T_HIT;
                 const int cx = r.ex - r.sx * r.kx, cy = r.ey - r.sy * r.ky, cz = r.ez - r.sz * r.kz;
