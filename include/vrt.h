@@ -234,7 +234,8 @@ int vrt_terrain_height(int32_t width, uint64_t seed, int32_t x, int32_t z);
  * tile counter, the staging image and streams of vrt_render_to_host, and the word
  * kernel's tile order (128 bytes per pixel tile).  Each word-kernel render sorts its tiles
  * into cost classes as they end, and the next word-kernel render of the same tile grid on
- * the same renderer launches them heaviest class first; the order changes no result.
+ * the same renderer launches them heaviest class first; the order changes no result (and
+ * without device memory for it, frames run in row order).
  * Creating the first renderer on a device also fills a 1 KiB table the pixel colour reads
  * (synchronises the device once).  One renderer per concurrently used stream. */
 int vrt_renderer_create(vrt_renderer** out);

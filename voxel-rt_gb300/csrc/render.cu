@@ -241,7 +241,7 @@ __global__ void __launch_bounds__(128) render_word_kernel(const int32_t* __restr
                 base += n;
             }
         }
-        if (b == 0)
+        if (b == 0 && p.class_count_clear)
             for (int c = 0; c < kTileClasses; c++) p.class_count_clear[c] = 0;
         s_tile = tile;
         s_cost = 0;
@@ -335,7 +335,7 @@ __global__ void __launch_bounds__(128) render_word_kernel(const int32_t* __restr
     const int wmax = __reduce_max_sync(0xffffffffu, valid ? res.steps : 0);
     if ((threadIdx.x & 31) == 0) atomicMax(&s_cost, wmax);
     __syncthreads();
-    if (threadIdx.x == 0) {
+    if (threadIdx.x == 0 && p.class_list_out) {
         const int c = tile_class(s_cost);
         p.class_list_out[c * p.tiles + atomicAdd(p.class_count_out + c, 1)] = tile;
     }
@@ -1511,9 +1511,16 @@ int vrt_renderer_destroy(vrt_renderer* r) {
 // The tile-order buffers of a word-kernel launch over grid g.  Frame f of a grid reads the
 // classes frame f-1 wrote (count buffer f%3, lists f%2), appends to count buffer (f+1)%3
 // and lists (f+1)%2, and clears count buffer (f+2)%3 for frame f+1: that buffer was last
-// read by frame f-1, which ended before frame f began (one stream per renderer).
+// read by frame f-1, which ended before frame f began (one stream per renderer).  The
+// order only speeds frames up: without room for its buffers the launch runs in row order.
 static int word_tile_order(vrt_renderer* r, dim3 g, cudaStream_t s, WordParams* p) {
     const int nt = (int)(g.x * g.y);
+    p->tiles = nt;
+    p->class_count_in = nullptr;
+    p->class_list_in = nullptr;
+    p->class_count_out = nullptr;
+    p->class_list_out = nullptr;
+    p->class_count_clear = nullptr;
     if (nt > r->tile_cap) {
         cudaFree(r->d_class_count);
         cudaFree(r->d_class_list);
@@ -1528,7 +1535,7 @@ static int word_tile_order(vrt_renderer* r, dim3 g, cudaStream_t s, WordParams* 
             r->d_class_count = nullptr;
             r->d_class_list = nullptr;
             r->tile_gx = r->tile_gy = 0;
-            return set_error(VRT_ENOMEM, "word kernel tile order: %s", cudaGetErrorString(e));
+            return VRT_OK;  // row order
         }
         r->tile_cap = nt;
         r->tile_gx = r->tile_gy = 0;
@@ -1543,7 +1550,6 @@ static int word_tile_order(vrt_renderer* r, dim3 g, cudaStream_t s, WordParams* 
     int* counts = r->d_class_count;
     int* lists = r->d_class_list;
     const size_t list = (size_t)kTileClasses * nt;
-    p->tiles = nt;
     p->class_count_in = f > 0 ? counts + (f % 3) * kTileClasses : nullptr;
     p->class_list_in = f > 0 ? lists + (f % 2) * list : nullptr;
     p->class_count_out = counts + ((f + 1) % 3) * kTileClasses;
