@@ -1006,7 +1006,12 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
         // (m == 0) it is 0.  Testing it without a branch on m pays: nearly every warp has a
         // lane inside a non-empty brick, so the branch would be taken anyway.
         r.bi = r.bi * one + (bx ? r.sx : (by ? r.sy * four : r.sz * sixteen));
-        const bool hb = (r.m >> (r.bi & 63)) & 1;
+        // PTX's shr.b64 clamps a shift count above 63 to 64 (a zero result): no mask of bi is
+        // needed.  bi leaves [0, 63] only in an empty box, where m is 0, or on a step out of
+        // the box, which the box test takes first.
+        uint64_t mb;
+        asm("shr.b64 %0, %1, %2;" : "=l"(mb) : "l"(r.m), "r"(r.bi));
+        const bool hb = mb & 1;
         if (((r.kx | r.ky | r.kz) < 0) | hb | last) {
             const int a = bx ? 0 : (by ? 1 : 2);
             const bool out = (r.kx | r.ky | r.kz) < 0;
