@@ -948,8 +948,8 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
     // (the step's term picked by the axis).  The compiler cannot turn it into a plain add,
     // so it issues on the FMA pipe, which the intersect adds leave mostly idle, instead of
     // the integer/logic pipe that bounds this loop.  (Doing the same for the box counters
-    // helped long empty boxes but cost more on the 1080p frame, so those stay plain
-    // subtractions of the axis flags.  Packing the three counters and the bit index into
+    // helped long empty boxes but cost more on the 1080p frame, so those stay predicated
+    // decrements.  Packing the three counters and the bit index into
     // one word, one add per step, took 3.7 % of the instructions away but was slower: all
     // of its work lands on the integer pipe.)
     const int one = P.one, four = P.four, sixteen = P.sixteen;
@@ -994,9 +994,9 @@ __device__ __forceinline__ int cast_box(const MaskParams& P, const int2* alive, 
         const bool bx = (r.tx < r.ty) & (r.tx < r.tz);
         const bool by = (r.ty < r.tx) & (r.ty < r.tz);  // false whenever bx holds, NaN included
         const bool bz = !(bx | by);
-        r.kx -= (int)bx;
-        r.ky -= (int)by;
-        r.kz -= (int)bz;
+        if (bx) r.kx -= 1;
+        if (by) r.ky -= 1;
+        if (bz) r.kz -= 1;
         bool last = false;  // DF: no iteration follows this one
         if (DF) {
             travelled = fadd(travelled, 1.0f);
