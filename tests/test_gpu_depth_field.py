@@ -234,3 +234,54 @@ def test_word_kernel_launches_heaviest_tiles_first(cuda, oracle):
         assert int(f["stats"][vrt.STAT_RAYS]) == o2["totals"]["rays"], tile
     assert_same_frame(o2, gpu_render(w, u2, 800, 600, kernel=vrt.KERNEL_WORD, renderer=r, tile=(32, 4)))
     r.close()
+
+
+def test_word_kernel_order_across_worlds_and_host_images(cuda, oracle):
+    """One renderer alternating between two depth-field worlds of one size, with images in
+    device memory, page-locked host memory and pageable host memory: every frame runs its
+    tiles in the order the previous frame (of the other world, or the other image kind)
+    recorded, and every frame equals the oracle's."""
+    import ctypes as C
+
+    # two worlds of one size: random_case's scene and camera, and sparse random voxels;
+    # 160x96 pixels make 120 tiles of 16x8 to order
+    words0, W, H, u0, _, _ = random_case(3)
+    width, height = 160, 96
+    rng = np.random.default_rng(77)
+    words1 = np.where(rng.random(W * H * W) < 0.06, 0x01000000 | rng.integers(0, 1 << 24, W * H * W),
+                      -1).astype(np.int32)
+    worlds = []
+    for words in (words0, words1):
+        w = make_world(words, W, H)
+        w.fix_depth_field()
+        worlds.append((w, w.download(np.empty_like(words))))
+    u0.aspectRatio = width / height
+    expect = [oracle.render(wd, W, H, u0, width, height)["rgba"] for _, wd in worlds]
+    r = vrt.Renderer()
+    o = vrt.RenderOpts()
+    o.kernel = vrt.KERNEL_WORD
+    n = width * height * 4
+    p = C.c_void_p()
+    vrt.check(vrt.lib().vrt_host_alloc(n, C.byref(p)))
+    try:
+        pinned = np.ctypeslib.as_array((C.c_uint8 * n).from_address(p.value))
+        pageable = np.zeros(n, np.uint8)
+        for frame in range(9):
+            k = frame % 2
+            w, _ = worlds[k]
+            kind = frame % 3
+            if kind == 0:
+                f = gpu_render(w, u0, width, height, kernel=vrt.KERNEL_WORD, debug=False, renderer=r)
+                img = f["rgba"]
+            elif kind == 1:
+                pinned[:] = 0
+                r.render_to_host(w, u0, width, height, p.value, o)
+                img = pinned.reshape(height, width, 4)
+            else:
+                pageable[:] = 0
+                r.render_to_host(w, u0, width, height, pageable.ctypes.data, o)
+                img = pageable.reshape(height, width, 4)
+            assert np.array_equal(img, expect[k]), (frame, kind)
+    finally:
+        vrt.check(vrt.lib().vrt_host_free(p))
+    r.close()
