@@ -204,12 +204,19 @@ COUNTER_SOURCES = [os.path.join("voxel-rt_gb300", "csrc", n) for n in ("render.c
 
 
 def kernel_source_hash() -> str:
-    """sha256 (16 hex digits) of the render kernels' sources, to match ncu counters to a build."""
+    """sha256 (16 hex digits) of the render kernels' code, to match ncu counters to a build.
+    Comments, whitespace at line ends and blank lines are left out (the sources have no
+    comment markers inside string literals), so a change of a comment keeps the counters;
+    any change of code drops them."""
     import hashlib
+    import re
     h = hashlib.sha256()
     for rel in COUNTER_SOURCES:
-        with open(os.path.join(ROOT, rel), "rb") as f:
-            h.update(f.read())
+        with open(os.path.join(ROOT, rel), encoding="utf-8") as f:
+            text = f.read()
+        text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+        lines = (re.sub(r"//.*", "", line).rstrip() for line in text.splitlines())
+        h.update("\n".join(line for line in lines if line).encode())
     return h.hexdigest()[:16]
 
 
