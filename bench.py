@@ -200,6 +200,9 @@ def run_reference(args):
     return 0
 
 
+# the ray tile each render kernel takes when the options name none
+DEFAULT_TILES = {"render_tiles_kernel": "8x16", "render_word_kernel": "16x8", "render_mask_kernel": "8x4"}
+
 COUNTER_SOURCES = [os.path.join("voxel-rt_gb300", "csrc", n) for n in ("render.cu", "shade_common.cuh")]
 
 
@@ -276,7 +279,8 @@ def main():
     ap.add_argument("--workload", default="full", choices=["full", "reference"],
                     help="full: the 1080p/16-light frame; reference: the reference's own world (initVoxels + "
                          "fixDepthField on the device) at 800x600, 384 steps, rendered by the kernel AUTO picks")
-    ap.add_argument("--tile", default="8x16")
+    ap.add_argument("--tile", default="default",
+                    help="ray tile WxH, or default: the kernel's own (8x16 tile kernel, 16x8 word kernel)")
     ap.add_argument("--refill", type=int, default=8)
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     args = ap.parse_args()
@@ -322,7 +326,8 @@ def main():
     opts = vrt.RenderOpts()
     opts.kernel = {"pixel": vrt.KERNEL_MASK_PIXEL, "mask": vrt.KERNEL_BITMASK, "word": vrt.KERNEL_WORD,
                    "auto": vrt.KERNEL_AUTO}[args.kernel]
-    opts.tile_w, opts.tile_h = (int(v) for v in args.tile.split("x"))
+    if args.tile != "default":
+        opts.tile_w, opts.tile_h = (int(v) for v in args.tile.split("x"))
     opts.refill_min = args.refill
     opts.blocks_per_sm = args.blocks_per_sm
     W, H = sc.width, sc.height
@@ -397,7 +402,7 @@ def main():
         "config": workload_config(sc, world_size),
         "frame": {"rays": rays, "dda_steps": steps, "dda_steps_performed": steps_performed,
                   "box_lookups": int(st_fast[4]), "primary_hits": hits, "pixels": pixels, "kernel": kname,
-                  "tile": args.tile, "refill_min": args.refill},
+                  "tile": args.tile if args.tile != "default" else DEFAULT_TILES[kname], "refill_min": args.refill},
         "clocks": clk, "gpu_launches": args.steps, "roofline": roofline, "e2e": e2e,
         "frame_ms_min": min(times), "frame_ms_max": max(times),
     }

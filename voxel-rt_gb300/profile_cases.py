@@ -24,7 +24,8 @@ commands in profiles/*.md name the case and the kernel (-k) they capture.
                  init_reference_trees), then fixDepthField over the whole world
   reference_frame  the reference app's first frame (its world with the depth field, camera
                  (195,55,155), 800x600, 384 steps), rendered as bench.py --workload reference
-                 does: the kernel AUTO picks (the word kernel), 8x16 pixel tiles, 2 launches
+                 does: the kernel AUTO picks (the word kernel) with its own 16x8 pixel tiles,
+                 2 launches
   all            every case above, one after the other
 
 Usage: python voxel-rt_gb300/profile_cases.py CASE
@@ -174,10 +175,9 @@ def case_reference_build(torch):
 def case_reference_frame(torch):
     w = _reference_world()
     u = scenes.reference_scene_uniforms()
-    o = vrt.RenderOpts()  # bench.py --workload reference: AUTO (the word kernel), 8x16 pixel tiles
-    o.tile_w, o.tile_h = 8, 16
+    o = vrt.RenderOpts()  # bench.py --workload reference: AUTO (the word kernel), its own 16x8 pixel tiles
     _render(torch, w, u, 800, 600, 2, o)
-    return "reference world, 800x600, AUTO kernel, 8x16 tiles: 2 frames"
+    return "reference world, 800x600, AUTO kernel, default (16x8) tiles: 2 frames"
 
 
 CASES = {name[5:]: fn for name, fn in globals().items() if name.startswith("case_")}
