@@ -69,3 +69,27 @@ def test_bench_reference_arm_under_torchrun_two_ranks(oracle):
     assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["value"] > 0
     assert d["config"]["world"] == "512x256x512" and d["config"]["parallelism"] == "replicas x2"
     assert d["e2e"]["h2d_bytes_per_step"] == 0 and d["cpu_baseline"]["kind"] == "port"
+
+
+def test_bench_reference_arm_under_two_ranks():
+    """bench.py --impl reference launched as the N=2 run is launched (torchrun, one process
+    per rank): rank 0 alone times the CPU restatement and prints the one JSON line, with
+    n_gpus = 2 and the same config keys as the N=1 line; rank 1 exits 0 without work."""
+    import json
+    import subprocess
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    cmd = [sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node=2",
+           "--master-addr=127.0.0.1", f"--master-port={_free_port()}",
+           os.path.join(root, "bench.py"), "--impl", "reference", "--gpus", "2", "--steps", "1", "--warmup", "0",
+           "--cpu-seconds", "0.4"]
+    p = subprocess.run(cmd, capture_output=True, text=True, timeout=600, cwd=root)
+    assert p.returncode == 0, p.stderr[-2000:]
+    lines = [json.loads(l) for l in p.stdout.splitlines() if l.startswith("{")]
+    assert len(lines) == 1, p.stdout
+    d = lines[0]
+    assert d["impl"] == "reference" and d["n_gpus"] == 2 and d["steps"] == 1
+    assert d["value"] > 0 and d["e2e"]["value"] == d["value"]
+    assert set(d["config"]) == {"workload", "world", "image", "max_steps", "local_lights", "seed", "l2",
+                                "parallelism"}
+    assert d["config"]["parallelism"] == "replicas x2"
