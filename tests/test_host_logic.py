@@ -104,3 +104,34 @@ def test_scene_helpers_in_the_oracle_library_match_libvrt(vrt_lib, oracle):
     h, loaded = out.stdout.split()
     import scenes
     assert h == scenes.words_hash(scenes.full(2, W=128, H=64).words) and loaded == "False"
+
+
+def test_counter_hash_follows_code_not_comments(tmp_path, monkeypatch):
+    """bench.py reports the issue-roofline fraction only when profiles/counters.json was
+    captured on the current kernel code.  The hash it compares leaves comments and blank
+    lines out, so an edited comment keeps the counters, while any change of code drops them;
+    and the committed counters match the committed kernels."""
+    import json
+    import shutil
+    import sys
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    if root not in sys.path:
+        sys.path.insert(0, root)
+    import bench
+    committed = bench.kernel_source_hash()
+    with open(os.path.join(root, "profiles", "counters.json")) as f:
+        counters = json.load(f)
+    assert all(e["source_sha16"] == committed for e in counters.values())
+
+    src = tmp_path / "voxel-rt_gb300" / "csrc"
+    src.mkdir(parents=True)
+    for rel in bench.COUNTER_SOURCES:
+        shutil.copy(os.path.join(root, rel), tmp_path / rel)
+    monkeypatch.setattr(bench, "ROOT", str(tmp_path))
+    assert bench.kernel_source_hash() == committed
+    cu = tmp_path / bench.COUNTER_SOURCES[0]
+    text = cu.read_text()
+    cu.write_text("// a new comment line\n\n/* and a block\n   comment */\n" + text.replace("\n", "  // note\n", 3))
+    assert bench.kernel_source_hash() == committed
+    cu.write_text(text.replace("__launch_bounds__(128, 7)", "__launch_bounds__(128, 8)"))
+    assert bench.kernel_source_hash() != committed
